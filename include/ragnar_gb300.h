@@ -1,0 +1,201 @@
+/*
+ * ragnar_gb300 -- C ABI of the GB300 (sm_103a) synchrotron hot path.
+ *
+ * Plain pointers and sizes only.  "device" pointers are CUDA device memory on
+ * the current device; "host" pointers are ordinary host memory.  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  Every entry
+ * point returns an rg_status; rg_last_error() gives the message of the last
+ * failure on the calling thread.  Unless stated otherwise, a call only enqueues
+ * work on `stream` and returns without synchronising.
+ *
+ * Each declaration cites the reference interface it replaces (file:line in the
+ * reference tree, paths under src/).
+ */
+#ifndef RAGNAR_GB300_H
+#define RAGNAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rg_status {
+  RG_OK              = 0,
+  RG_ERR_ARGUMENT    = 1, /* invalid argument; the reference throws std::runtime_error */
+  RG_ERR_CUDA        = 2, /* a CUDA runtime/driver call failed */
+  RG_ERR_TIMEOUT     = 3, /* a bounded on-device wait gave up; results are invalid */
+  RG_ERR_UNSUPPORTED = 4, /* configuration outside what this build supports */
+  RG_ERR_RANGE       = 5  /* the reference throws std::range_error / out_of_range */
+} rg_status;
+
+/* Table modes for the spectrum plans. */
+enum {
+  RG_TABLE_REFERENCE = 0, /* the reference's 200-point F table, piecewise linear in log10 x */
+  RG_TABLE_SMOOTH    = 1  /* exact F on a fine log grid, C1 cubic Hermite (differentiable) */
+};
+
+/* --------------------------------------------------------------------------
+ * Runtime
+ * ------------------------------------------------------------------------ */
+
+/* rg.Initialize (pyinterface.cpp:30-38): select `device`, create the context and
+ * build the default F table.  Idempotent. */
+int rg_init(int device);
+
+/* rg.Finalize (pyinterface.cpp:40-49): release cached plans and tables. */
+int rg_finalize(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* rg_last_error(void);
+
+/* Number of streaming multiprocessors of the current device (grid sizing). */
+int rg_device_sm_count(int* sms);
+
+/* Device memory helpers standing in for Kokkos::View allocation and
+ * deep_copy (array.hpp:21-30, array.cpp:46-51). */
+int rg_malloc(void** ptr, size_t bytes);
+int rg_free(void* ptr);
+int rg_memcpy_htod(void* dst, const void* src, size_t bytes, void* stream);
+int rg_memcpy_dtoh(void* dst, const void* src, size_t bytes, void* stream);
+int rg_memcpy_dtod(void* dst, const void* src, size_t bytes, void* stream);
+int rg_memset(void* dst, int value, size_t bytes, void* stream);
+int rg_stream_synchronize(void* stream);
+
+/* --------------------------------------------------------------------------
+ * Grids (host)
+ * ------------------------------------------------------------------------ */
+
+/* Logspace (snippets.cpp:39-62): pow(10, log10f(a) + i*log10f(b/a)/(n-1)) in the
+ * reference's float/double mix; writes `num` floats to host `out`.  Errors as the
+ * reference: start/stop must be > 0 and start < stop. */
+int rg_logspace(float start, float stop, int64_t num, float* out);
+
+/* Linspace (snippets.cpp:21-37): start + i*(stop-start)/(num-1); start < stop. */
+int rg_linspace(float start, float stop, int64_t num, float* out);
+
+/* --------------------------------------------------------------------------
+ * Synchrotron kernel function F(x) = x * int_x^inf K_{5/3}
+ * ------------------------------------------------------------------------ */
+
+/* Ffunc_integrand (synchrotron.cpp:28-46) for n device values x -> device y,
+ * evaluated on the GPU in FP64 (own K_{5/3} quadrature) with the reference's
+ * float rounding steps. */
+int rg_ffunc_integrand(const float* x, int64_t n, float* y, void* stream);
+
+/* TabulateFfunc (synchrotron.cpp:48-65): the n-node table on Logspace(xmin, xmax, n)
+ * (x nodes computed on the host exactly as Logspace does, y on the GPU in FP64).
+ * x and y are device arrays of n floats. */
+int rg_ffunc_table(int64_t n, float xmin, float xmax, float* x, float* y, void* stream);
+
+/* --------------------------------------------------------------------------
+ * Particle synchrotron spectrum
+ * ------------------------------------------------------------------------ */
+
+/* Device SoA view of Particles<D> (particles.hpp:18-72): U, E, B as three
+ * components each (NULL E or B component = 0, as unset components of the
+ * reference are zero), optional per-particle weight (NULL = 1; the reference has
+ * no weight). */
+typedef struct rg_particles {
+  const float* u[3];
+  const float* e[3];
+  const float* b[3];
+  const float* w;
+  int64_t      n;
+} rg_particles;
+
+typedef struct rg_spectrum_plan rg_spectrum_plan;
+
+/* Prepares a spectrum over `nbins` host photon energies (any positive values;
+ * non-positive bins yield 0) for the scalars of SynchrotronSpectrum<D>
+ * (synchrotron.cpp:107-145): B0, g_syn, e_syn_at_g_syn.  `table_mode` is one of
+ * RG_TABLE_*.  Allocates the plan's device state.  A plan may be run on one
+ * stream at a time. */
+int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_syn,
+                            float e_syn_at_g_syn, int32_t table_mode,
+                            rg_spectrum_plan** plan);
+int rg_spectrum_plan_destroy(rg_spectrum_plan* plan);
+
+/* Reserves scratch for batched runs of up to `max_segments` segments (call before
+ * capturing a batched run into a CUDA graph). */
+int rg_spectrum_plan_reserve(rg_spectrum_plan* plan, int32_t max_segments);
+
+/* Synchronises `stream` and reports a failure recorded on the device by earlier
+ * runs of `plan` (bad segment offsets: RG_ERR_ARGUMENT; a bounded wait that gave
+ * up: RG_ERR_TIMEOUT, outputs are NaN).  Clears the record.  The reference has no
+ * device-side failure path; this replaces the synchronous Kokkos::fence()
+ * (synchrotron.cpp:142) as the point where errors surface. */
+int rg_spectrum_plan_check(rg_spectrum_plan* plan, void* stream);
+
+/* The fused forward: out[b] = e_b * sum_p w_p chiR_p F(e_b / e_peak_p) for the
+ * particles in `p` (sync::Kernel<D>::operator(), synchrotron.hpp:145-172, summed
+ * as SynchrotronSpectrum<D> does).  `out` is nbins device floats. */
+int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* out,
+                    void* stream);
+
+/* Batched form: segment s covers particles [offsets[s], offsets[s+1]) of `p`
+ * (device array of nseg+1 non-decreasing offsets); out is [nseg x nbins] device
+ * floats.  One persistent launch for all segments; no host synchronisation, so
+ * the call can be captured into a CUDA graph after rg_spectrum_plan_reserve.
+ * Extension: the reference computes one spectrum per call. */
+int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p,
+                            const int64_t* offsets, int32_t nseg, float* out, void* stream);
+
+/* The plain one-spectrum-per-launch kernel (thread per particle, per-eval
+ * interpolation as the reference writes it); the baseline the fused kernel is
+ * measured against.  Reference table mode only. */
+int rg_spectrum_run_plain(const rg_spectrum_plan* plan, const rg_particles* p, float* out,
+                          void* stream);
+
+/* One-shot drop-in for SynchrotronSpectrum<D> (synchrotron.cpp:107-145): plan
+ * (cached by arguments) + run, reference table mode. */
+int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nbins, float B0,
+                            float g_syn, float e_syn_at_g_syn, float* out, void* stream);
+
+/* --------------------------------------------------------------------------
+ * Spectrum from a tabulated distribution
+ * ------------------------------------------------------------------------ */
+
+/* SynchrotronSpectrumFromDist (synchrotron.cpp:69-105, sync::KernelFromDist
+ * synchrotron.hpp:72-95): gbeta (device, ng) and f (device, ng) describe the
+ * distribution; J_g = gbeta_g if log_spaced else 1; bins is host (nbins);
+ * out is nbins device floats. */
+int rg_synchrotron_spectrum_from_dist(const float* gbeta, const float* f, int32_t ng,
+                                      int32_t log_spaced, const float* bins, int32_t nbins,
+                                      float g_syn, float e_syn_at_g_syn, float* out,
+                                      void* stream);
+
+/* --------------------------------------------------------------------------
+ * Energy distribution (histogram)
+ * ------------------------------------------------------------------------ */
+
+/* Bin thresholds used by rg_energy_distribution: thr[k] (k >= 1) is the smallest
+ * non-negative float |u|^2 whose reference bin index (particles.cpp:231-243) is
+ * >= k; thr[0] = 0; nan_index receives the index the host's build of that
+ * expression gives a NaN energy.  bins is host (nbins); thr is host (nbins). */
+int rg_energy_thresholds(const float* bins, int32_t nbins, int32_t fourvel, float* thr,
+                         int32_t* nan_index);
+
+/* Particles<D>::energyDistribution (particles.cpp:189-260): energy = |u| (fourvel)
+ * or sqrt(1+u^2); bin index always from log10 (even for linear bins), clamped
+ * into [0, n-1]; hist[k] = sum 1/energy (log_spaced) or the count.  bins is host
+ * (nbins); hist is nbins device floats; counts (nullable) receives exact
+ * uint64 counts per bin. */
+int rg_energy_distribution(const float* ux, const float* uy, const float* uz, int64_t n,
+                           const float* bins, int32_t nbins, int32_t log_spaced,
+                           int32_t fourvel, float* hist, uint64_t* counts, void* stream);
+
+/* --------------------------------------------------------------------------
+ * Diagnostics: the FP64 quadratures of the table builders evaluated on the
+ * host (same code as on the GPU); K_{5/3}(x) and F(x) = x int_x^inf K_{5/3}.
+ * The reference evaluates K_{5/3} with std::cyl_bessel_k (synchrotron.cpp:38).
+ * ------------------------------------------------------------------------ */
+double rg_debug_bessel_k53(double x);
+double rg_debug_exact_F(double x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAGNAR_GB300_H */

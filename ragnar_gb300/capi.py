@@ -1,0 +1,175 @@
+"""ctypes binding of the C ABI (``include/ragnar_gb300.h``).
+
+Used by the torch extension, the tests and the benchmark to call the library
+exactly as a foreign caller would: plain pointers, sizes and a stream handle.
+Device buffers can be anything exposing a device address (torch tensors via
+``data_ptr()``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libragnar_gb300.so")
+HEADER = os.path.join(os.path.dirname(_HERE), "include", "ragnar_gb300.h")
+
+RG_OK = 0
+RG_ERR_ARGUMENT = 1
+RG_ERR_CUDA = 2
+RG_ERR_TIMEOUT = 3
+RG_ERR_UNSUPPORTED = 4
+RG_ERR_RANGE = 5
+RG_TABLE_REFERENCE = 0
+RG_TABLE_SMOOTH = 1
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_f32 = ctypes.c_float
+_int = ctypes.c_int
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+
+class RgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+class Particles(ctypes.Structure):
+    """rg_particles: device SoA pointers (0 = null)."""
+
+    _fields_ = [("u", _vp * 3), ("e", _vp * 3), ("b", _vp * 3), ("w", _vp), ("n", _i64)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} not built; run `python -m ragnar_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L: ctypes.CDLL) -> None:
+    sig = {
+        "rg_init": [_int],
+        "rg_finalize": [],
+        "rg_device_sm_count": [ctypes.POINTER(_int)],
+        "rg_malloc": [ctypes.POINTER(_vp), ctypes.c_size_t],
+        "rg_free": [_vp],
+        "rg_memcpy_htod": [_vp, _vp, ctypes.c_size_t, _vp],
+        "rg_memcpy_dtoh": [_vp, _vp, ctypes.c_size_t, _vp],
+        "rg_memcpy_dtod": [_vp, _vp, ctypes.c_size_t, _vp],
+        "rg_memset": [_vp, _int, ctypes.c_size_t, _vp],
+        "rg_stream_synchronize": [_vp],
+        "rg_logspace": [_f32, _f32, _i64, _vp],
+        "rg_linspace": [_f32, _f32, _i64, _vp],
+        "rg_ffunc_integrand": [_vp, _i64, _vp, _vp],
+        "rg_ffunc_table": [_i64, _f32, _f32, _vp, _vp, _vp],
+        "rg_spectrum_plan_create": [_vp, _i32, _f32, _f32, _f32, _i32, ctypes.POINTER(_vp)],
+        "rg_spectrum_plan_destroy": [_vp],
+        "rg_spectrum_plan_reserve": [_vp, _i32],
+        "rg_spectrum_plan_check": [_vp, _vp],
+        "rg_spectrum_run": [_vp, ctypes.POINTER(Particles), _vp, _vp],
+        "rg_spectrum_run_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp],
+        "rg_spectrum_run_plain": [_vp, ctypes.POINTER(Particles), _vp, _vp],
+        "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
+        "rg_synchrotron_spectrum_from_dist": [_vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _vp, _vp],
+        "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
+        "rg_energy_distribution": [_vp, _vp, _vp, _i64, _vp, _i32, _i32, _i32, _vp, _vp, _vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = _int
+    L.rg_last_error.argtypes = []
+    L.rg_last_error.restype = ctypes.c_char_p
+    for name in ("rg_debug_bessel_k53", "rg_debug_exact_F"):
+        fn = getattr(L, name)
+        fn.argtypes = [ctypes.c_double]
+        fn.restype = ctypes.c_double
+
+
+def check(status: int) -> None:
+    if status != RG_OK:
+        msg = lib().rg_last_error().decode(errors="replace")
+        raise RgError(status, msg)
+
+
+def header_functions(path: str = HEADER) -> list[str]:
+    """Names of every function the C ABI header declares."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(rg_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def addr(t) -> int:
+    """Device address of a tensor-like (0 for None)."""
+    if t is None:
+        return 0
+    if isinstance(t, int):
+        return t
+    return int(t.data_ptr())
+
+
+def particles(u, b=None, e=None, w=None, n=None) -> Particles:
+    """Build an rg_particles from 3-sequences of device tensors (or None)."""
+    p = Particles()
+    for d in range(3):
+        p.u[d] = addr(u[d])
+        p.e[d] = addr(e[d]) if e is not None else 0
+        p.b[d] = addr(b[d]) if b is not None else 0
+    p.w = addr(w)
+    p.n = int(n if n is not None else u[0].numel())
+    return p
+
+
+class SpectrumPlan:
+    """Owning wrapper of rg_spectrum_plan."""
+
+    def __init__(self, bins, B0: float, g_syn: float, eps: float, mode: int = RG_TABLE_REFERENCE):
+        import numpy as np  # noqa: PLC0415
+
+        self.bins = np.ascontiguousarray(bins, dtype=np.float32)
+        self.nbins = len(self.bins)
+        h = _vp()
+        check(lib().rg_spectrum_plan_create(self.bins.ctypes.data, self.nbins, B0, g_syn, eps, mode,
+                                            ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, prt: Particles, out, stream: int = 0) -> None:
+        check(lib().rg_spectrum_run(self.handle, ctypes.byref(prt), addr(out), stream))
+
+    def run_plain(self, prt: Particles, out, stream: int = 0) -> None:
+        check(lib().rg_spectrum_run_plain(self.handle, ctypes.byref(prt), addr(out), stream))
+
+    def run_batched(self, prt: Particles, offsets, nseg: int, out, stream: int = 0) -> None:
+        check(lib().rg_spectrum_run_batched(self.handle, ctypes.byref(prt), addr(offsets), nseg,
+                                            addr(out), stream))
+
+    def reserve(self, nseg: int) -> None:
+        check(lib().rg_spectrum_plan_reserve(self.handle, nseg))
+
+    def check(self, stream: int = 0) -> None:
+        check(lib().rg_spectrum_plan_check(self.handle, stream))
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().rg_spectrum_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # noqa: D105
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

@@ -1,0 +1,320 @@
+// Particles<D>::energyDistribution (particles.cpp:189-260) on sm_103a.
+//
+// The reference computes Usqr = ux*ux + uy*uy + uz*uz in float, then the bin
+// index through a double expression (double log10 of energy/emin, float log10
+// of emax/emin), clamping out-of-range energies into bins 0 and n-1.  Because that
+// index is a non-decreasing function of the float Usqr alone, the host finds,
+// for every k, the smallest float Usqr whose index is >= k (binary search over
+// float bit patterns with the reference's own expression).  The GPU computes
+// Usqr with the same rounding steps, estimates the index in FP32 and corrects
+// it against those thresholds, so every particle lands in exactly the bin the
+// reference picks and the counts are bit-exact.
+//
+// Log-spaced bins add float(1.0 / energy): for |u| energies that is the
+// correctly rounded reciprocal of sqrtf(Usqr) (double rounding of one division
+// of floats through double is innocuous); for sqrt(1 + Usqr) energies it is a
+// double-float Newton step of rsqrt rounded to float.  Sums are accumulated in
+// FP32 shared-memory bins flushed to FP64 every chunk, then across blocks in
+// FP64 in a fixed order.
+#include "rg_common.cuh"
+#include "rg_internal.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace rg {
+
+  namespace {
+
+    constexpr int kHistThreads   = 256;
+    constexpr int kHistMaxBins   = 4096;
+    constexpr int kFlushParticles = 4096; // per block between FP32 -> FP64 flushes
+
+    // particles.cpp:224-253, the index of one particle given its float Usqr.
+    std::size_t ref_energy_index(float Usqr, bool fourvel, float emin, float emax, std::size_t n) {
+      const double energy = fourvel ? static_cast<double>(std::sqrt(Usqr)) : std::sqrt(1.0 + Usqr);
+      if (energy < emin) {
+        return 0;
+      } else if (energy >= emax) {
+        return n - 1;
+      }
+      const auto ei = static_cast<std::size_t>(static_cast<float>(n - 1) *
+                                               std::fabs(std::log10(energy / emin)) /
+                                               std::log10(emax / emin));
+      return ei > n - 1 ? n - 1 : ei;
+    }
+
+    float bits_to_float(uint32_t b) {
+      float f;
+      std::memcpy(&f, &b, 4);
+      return f;
+    }
+
+    struct HistParams {
+      const float*    ux;
+      const float*    uy;
+      const float*    uz;
+      int64_t         n;
+      int             nbins;
+      int             fourvel;
+      int             log_spaced;
+      const float*    thr;      // nbins thresholds: thr[k] = smallest Usqr with index >= k (thr[0] = 0)
+      int             nan_index;
+      float           est_a, est_c; // FP32 index estimate: a * log2(E^2) + c
+      unsigned long long* part_counts; // [grid][nbins]
+      double*         part_sums;       // [grid][nbins]
+    };
+
+    __device__ __forceinline__ int bin_of(float U, const HistParams& p, const float* thr) {
+      if (U != U) {
+        return p.nan_index;
+      }
+      const int   nm1 = p.nbins - 1;
+      const float l   = __log2f(p.fourvel ? U : __fadd_rn(1.0f, U));
+      float       t   = fmaf(p.est_a, l, p.est_c);
+      int         g   = 0;
+      if (t > 0.0f) {
+        g = t >= static_cast<float>(nm1) ? nm1 : static_cast<int>(t);
+      }
+      // correct the estimate against the exact thresholds (bounded)
+      for (int it = 0; it < p.nbins && g < nm1 && thr[g + 1] <= U; ++it) {
+        ++g;
+      }
+      for (int it = 0; it < p.nbins && g > 0 && thr[g] > U; ++it) {
+        --g;
+      }
+      return g;
+    }
+
+    // float(1.0 / sqrt(1.0 + U)) without FP64: one Newton step in double-float.
+    __device__ __forceinline__ float inv_sqrt_one_plus(float U) {
+      const ff    s  = two_sum(1.0f, U);
+      const float r0 = rsqrtf(s.hi);
+      // e = 1 - s r0^2 in double-float, r = r0 + r0 e / 2
+      const ff r2 = two_prod(r0, r0);
+      const ff sr = ff_mul(s, r2);
+      const float e = __fadd_rn(__fsub_rn(1.0f, sr.hi), -sr.lo);
+      return __fmaf_rn(__fmul_rn(0.5f, r0), e, r0);
+    }
+
+    __global__ void __launch_bounds__(kHistThreads)
+      histogram_kernel(const __grid_constant__ HistParams p) {
+      extern __shared__ __align__(16) unsigned char smem[];
+      const int nb      = p.nbins;
+      float*    thr     = reinterpret_cast<float*>(smem);
+      unsigned* cnt     = reinterpret_cast<unsigned*>(thr + nb);
+      float*    sum32   = reinterpret_cast<float*>(cnt + nb);
+      double*   sum64   = reinterpret_cast<double*>(smem + ((3 * sizeof(float) * nb + 15) & ~size_t(15)));
+      for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        thr[i]   = p.thr[i];
+        cnt[i]   = 0u;
+        sum32[i] = 0.0f;
+        sum64[i] = 0.0;
+      }
+      __syncthreads();
+
+      // contiguous range of particles per block, in rounds of kFlushParticles
+      const int64_t G       = gridDim.x;
+      const int64_t per     = ((p.n + G - 1) / G + 3) & ~int64_t(3);
+      const int64_t begin   = min(p.n, per * blockIdx.x);
+      const int64_t end     = min(p.n, begin + per);
+      const bool    vec_ok  = ((reinterpret_cast<uintptr_t>(p.ux) | reinterpret_cast<uintptr_t>(p.uy) |
+                            reinterpret_cast<uintptr_t>(p.uz)) & 15) == 0;
+
+      for (int64_t r0 = begin; r0 < end; r0 += kFlushParticles) {
+        const int64_t r1 = min(end, r0 + kFlushParticles);
+        auto          one = [&](float x, float y, float z) {
+          const float U = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+          const int   k = bin_of(U, p, thr);
+          atomicAdd(&cnt[k], 1u);
+          if (p.log_spaced) {
+            const float v = p.fourvel ? __frcp_rn(sqrtf(U)) : inv_sqrt_one_plus(U);
+            atomicAdd(&sum32[k], v);
+          }
+        };
+        if (vec_ok) {
+          // 4 particles per thread with 128-bit loads (begin and per are multiples of 4)
+          const int64_t nv = (r1 - r0) / 4;
+          for (int64_t v = threadIdx.x; v < nv; v += blockDim.x) {
+            const int64_t i  = r0 + 4 * v;
+            const float4  X  = __ldcs(reinterpret_cast<const float4*>(p.ux + i));
+            const float4  Y  = __ldcs(reinterpret_cast<const float4*>(p.uy + i));
+            const float4  Z  = __ldcs(reinterpret_cast<const float4*>(p.uz + i));
+            one(X.x, Y.x, Z.x);
+            one(X.y, Y.y, Z.y);
+            one(X.z, Y.z, Z.z);
+            one(X.w, Y.w, Z.w);
+          }
+          for (int64_t i = r0 + 4 * nv + threadIdx.x; i < r1; i += blockDim.x) {
+            one(p.ux[i], p.uy[i], p.uz[i]);
+          }
+        } else {
+          for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            one(p.ux[i], p.uy[i], p.uz[i]);
+          }
+        }
+        if (p.log_spaced) {
+          __syncthreads();
+          for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+            sum64[i] += static_cast<double>(sum32[i]);
+            sum32[i] = 0.0f;
+          }
+        }
+        __syncthreads();
+      }
+      for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        p.part_counts[static_cast<int64_t>(blockIdx.x) * nb + i] = cnt[i];
+        p.part_sums[static_cast<int64_t>(blockIdx.x) * nb + i]   = sum64[i];
+      }
+    }
+
+    __global__ void histogram_reduce_kernel(const unsigned long long* __restrict__ pc,
+                                            const double* __restrict__ ps, int grid, int nbins,
+                                            int log_spaced, float* __restrict__ hist,
+                                            unsigned long long* __restrict__ counts) {
+      const int k = blockIdx.x * blockDim.x + threadIdx.x;
+      if (k >= nbins) {
+        return;
+      }
+      unsigned long long c = 0;
+      double             s = 0.0;
+      for (int b = 0; b < grid; ++b) {
+        c += pc[static_cast<int64_t>(b) * nbins + k];
+        s += ps[static_cast<int64_t>(b) * nbins + k];
+      }
+      hist[k] = log_spaced ? __double2float_rn(s) : static_cast<float>(c);
+      if (counts) {
+        counts[k] = c;
+      }
+    }
+
+  } // namespace
+
+  // Thresholds thr[k] (k = 1..n-1): the smallest non-negative float Usqr whose
+  // reference index is >= k (+inf if none); thr[0] = 0.  Exposed for tests.
+  void energy_thresholds(const float* bins, int n, bool fourvel, std::vector<float>& thr,
+                         int& nan_index, float& emin, float& emax) {
+    emin = std::numeric_limits<float>::max();
+    emax = std::numeric_limits<float>::lowest();
+    for (int i = 0; i < n; ++i) {
+      emin = std::min(emin, bins[i]);
+      emax = std::max(emax, bins[i]);
+    }
+    thr.assign(n, 0.0f);
+    const uint32_t inf_bits = 0x7f800000u;
+    for (int k = 1; k < n; ++k) {
+      // smallest bit pattern b in [0, inf] with index(b) >= k
+      uint32_t lo = 0, hi = inf_bits;
+      if (ref_energy_index(bits_to_float(hi), fourvel, emin, emax, n) < static_cast<std::size_t>(k)) {
+        thr[k] = std::numeric_limits<float>::infinity();
+        continue;
+      }
+      while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (ref_energy_index(bits_to_float(mid), fourvel, emin, emax, n) >= static_cast<std::size_t>(k)) {
+          hi = mid;
+        } else {
+          lo = mid + 1;
+        }
+      }
+      thr[k] = bits_to_float(lo);
+    }
+    nan_index = static_cast<int>(
+      ref_energy_index(std::numeric_limits<float>::quiet_NaN(), fourvel, emin, emax, n));
+  }
+
+} // namespace rg
+
+extern "C" {
+
+int rg_energy_thresholds(const float* bins, int32_t nbins, int32_t fourvel, float* thr,
+                         int32_t* nan_index) {
+  if (nbins < 1 || !bins || !thr) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_energy_thresholds: bad arguments");
+  }
+  std::vector<float> t;
+  int                ni = 0;
+  float              emin, emax;
+  rg::energy_thresholds(bins, nbins, fourvel != 0, t, ni, emin, emax);
+  std::copy(t.begin(), t.end(), thr);
+  if (nan_index) {
+    *nan_index = ni;
+  }
+  return RG_OK;
+}
+
+int rg_energy_distribution(const float* ux, const float* uy, const float* uz, int64_t n,
+                           const float* bins, int32_t nbins, int32_t log_spaced, int32_t fourvel,
+                           float* hist, uint64_t* counts, void* stream) {
+  rg::clear_error();
+  if (nbins < 1 || !bins || !hist || n < 0 || (n > 0 && (!ux || !uy || !uz))) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_energy_distribution: bad arguments");
+  }
+  if (nbins > rg::kHistMaxBins) {
+    return rg::set_error(RG_ERR_UNSUPPORTED, "energyDistribution supports at most 4096 bins");
+  }
+  auto               s = static_cast<cudaStream_t>(stream);
+  std::vector<float> thr;
+  int                nan_index = 0;
+  float              emin, emax;
+  rg::energy_thresholds(bins, nbins, fourvel != 0, thr, nan_index, emin, emax);
+
+  rg::DeviceContext* ctx = nullptr;
+  RG_TRY(rg::context(&ctx));
+  const size_t smem = ((3 * sizeof(float) * nbins + 15) & ~size_t(15)) + sizeof(double) * nbins;
+  if (smem > 48 * 1024) {
+    RG_CUDA_TRY(cudaFuncSetAttribute(rg::histogram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  }
+  int per_sm = 0;
+  RG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rg::histogram_kernel,
+                                                            rg::kHistThreads, smem));
+  per_sm = std::max(1, std::min(per_sm, 8));
+  const int64_t want = std::max<int64_t>(1, (n + 4095) / 4096);
+  const int     G    = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(ctx->sms) * per_sm));
+
+  // one allocation for thresholds and per-block partials, freed stream-ordered
+  const size_t off_pc = 256 * ((sizeof(float) * nbins + 255) / 256);
+  const size_t off_ps = off_pc + sizeof(unsigned long long) * static_cast<size_t>(G) * nbins;
+  const size_t bytes  = off_ps + sizeof(double) * static_cast<size_t>(G) * nbins;
+  unsigned char* buf  = nullptr;
+  RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
+  RG_CUDA_TRY(cudaMemcpyAsync(buf, thr.data(), sizeof(float) * nbins, cudaMemcpyHostToDevice, s));
+
+  rg::HistParams p {};
+  p.ux         = ux;
+  p.uy         = uy;
+  p.uz         = uz;
+  p.n          = n;
+  p.nbins      = nbins;
+  p.fourvel    = fourvel ? 1 : 0;
+  p.log_spaced = log_spaced ? 1 : 0;
+  p.thr        = reinterpret_cast<const float*>(buf);
+  p.nan_index  = nan_index;
+  // estimate: index ~ (n-1) log(E/emin) / log(emax/emin), log2(E) = log2(E^2) / 2
+  const double span = std::log2(static_cast<double>(emax) / static_cast<double>(emin));
+  if (emin > 0 && std::isfinite(span) && span > 0) {
+    p.est_a = static_cast<float>((nbins - 1) * 0.5 / span);
+    p.est_c = static_cast<float>(-(nbins - 1) * std::log2(static_cast<double>(emin)) / span);
+  } else {
+    p.est_a = 0.0f;
+    p.est_c = 0.0f;
+  }
+  p.part_counts = reinterpret_cast<unsigned long long*>(buf + off_pc);
+  p.part_sums   = reinterpret_cast<double*>(buf + off_ps);
+  rg::histogram_kernel<<<G, rg::kHistThreads, smem, s>>>(p);
+  RG_CUDA_TRY(cudaGetLastError());
+  rg::histogram_reduce_kernel<<<(nbins + 127) / 128, 128, 0, s>>>(
+    p.part_counts, p.part_sums, G, nbins, p.log_spaced, hist,
+    reinterpret_cast<unsigned long long*>(counts));
+  RG_CUDA_TRY(cudaGetLastError());
+  RG_CUDA_TRY(cudaFreeAsync(buf, s));
+  // thr (host) must outlive the asynchronous copy above
+  RG_CUDA_TRY(cudaStreamSynchronize(s));
+  return RG_OK;
+}
+
+} // extern "C"

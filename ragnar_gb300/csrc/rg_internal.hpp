@@ -1,0 +1,90 @@
+// Internal host-side declarations of the ragnar_gb300 library.
+#pragma once
+
+#include "ragnar_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace rg {
+
+  // ---- errors ---------------------------------------------------------------
+  int  set_error(int status, const std::string& msg);
+  int  cuda_error(cudaError_t e, const char* what);
+  void clear_error();
+
+#define RG_CUDA_TRY(expr)                                                               \
+  do {                                                                                  \
+    cudaError_t rg_e_ = (expr);                                                         \
+    if (rg_e_ != cudaSuccess) {                                                         \
+      return ::rg::cuda_error(rg_e_, #expr);                                            \
+    }                                                                                   \
+  } while (0)
+
+#define RG_TRY(expr)                                                                    \
+  do {                                                                                  \
+    int rg_s_ = (expr);                                                                 \
+    if (rg_s_ != RG_OK) {                                                               \
+      return rg_s_;                                                                     \
+    }                                                                                   \
+  } while (0)
+
+  // ---- F tables ---------------------------------------------------------------
+
+  // Fixed-point table coordinate: T = t * 2^kFrac with t the (fractional) node
+  // index.  The reference table's segments occupy entries [0, n-2] of a
+  // 1024-entry table whose other entries are zero, so any 32-bit T maps to a
+  // valid entry (T >> kFrac < 1024).
+  constexpr int      kFrac        = 22;
+  constexpr int      kRefEntries  = 1024;
+  constexpr uint32_t kFracMask    = (1u << kFrac) - 1u;
+  // c1 is stored pre-multiplied by 2^127: a denormal built from the fraction
+  // bits (bits * 2^-149) times c1 * 2^127 equals frac * c1.
+  constexpr double   kSlopeScale  = 1.7014118346046923e38; // 2^127
+
+  // Smooth (differentiable) table: exact F on a log grid, cubic Hermite segments.
+  constexpr int    kSmoothSegments = 4096;
+  constexpr double kSmoothXmin     = 1e-6;
+  constexpr double kSmoothXmax     = 100.0;
+
+  struct RefTable {
+    int     n      = 0;       // nodes
+    float   xmin   = 0, xmax = 0;
+    float*  d_x    = nullptr; // n nodes
+    float*  d_y    = nullptr; // n values
+    float2* d_coef = nullptr; // kRefEntries (c0, c1 * 2^127) per segment
+    double  ln_xmin = 0, dln = 0; // ideal grid: t = (ln x - ln_xmin) / dln
+    std::vector<float> h_x, h_y;
+  };
+
+  struct SmoothTable {
+    float4* d_coef  = nullptr; // kSmoothSegments (c0, c1, c2, c3) in tau
+    double  ln_xmin = 0, dln = 0;
+  };
+
+  struct DeviceContext {
+    int         device = -1;
+    int         sms    = 0;
+    RefTable    ref;
+    SmoothTable smooth;
+    bool        ref_ready = false, smooth_ready = false;
+  };
+
+  // Context of the current device (created on first use; builds tables lazily).
+  int context(DeviceContext** ctx);
+  int reference_table(const RefTable** t);
+  int smooth_table(const SmoothTable** t);
+
+  // Builds the reference table on `n` nodes of Logspace(xmin, xmax) (FP64 on the GPU).
+  int build_reference_table(int n, float xmin, float xmax, RefTable& t, cudaStream_t s);
+  int build_smooth_table(SmoothTable& t, cudaStream_t s);
+  void free_tables(DeviceContext& c);
+
+  // Host grids with the reference's float/double arithmetic.
+  float logspace_point(float start, float stop, std::size_t num, std::size_t i);
+
+} // namespace rg
