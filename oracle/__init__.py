@@ -60,6 +60,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.orc_sync_spectrum_batched_f64.argtypes = P10 + [_i64p, _i64] + tail + [_f64p, _int]
     L.orc_energy_bin_index.argtypes = [_f32, _f32, _f32, _int, _f32, _f32, _i64]
     L.orc_energy_bin_index.restype = _i64
+    L.orc_energy_bin_index_usqr.argtypes = [_f32, _int, _f32, _f32, _i64]
+    L.orc_energy_bin_index_usqr.restype = _i64
     L.orc_energy_distribution.argtypes = [_f32p, _f32p, _f32p, _i64, _f32p, _i64, _int, _int,
                                           _f32p, _f64p, _i64p, _int]
     fd = [_f32p, _f32p, _i64, _i64, _int, _f32p, _i64, _f32, _f32, _f32p, _f32p, _i64]
@@ -167,6 +169,11 @@ def energy_distribution(ux, uy, uz, bins, log_spaced: bool, fourvel: bool = True
 
 def energy_bin_index(ux, uy, uz, fourvel, emin, emax, n) -> int:
     return int(lib().orc_energy_bin_index(ux, uy, uz, int(fourvel), emin, emax, n))
+
+
+def energy_bin_index_usqr(usqr, fourvel, emin, emax, n) -> int:
+    """Reference bin index (particles.cpp:229-243) of one float |u|^2."""
+    return int(lib().orc_energy_bin_index_usqr(usqr, int(fourvel), emin, emax, n))
 
 
 # ---- FromDist -----------------------------------------------------------------------

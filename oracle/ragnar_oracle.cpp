@@ -101,6 +101,24 @@ namespace {
     e_peak          = eps * gamma * gamma * chiR / (g_syn * g_syn);
   }
 
+  // The reference's own rounding of the same (synchrotron.hpp:230-231): chiR is a
+  // float output parameter, so e_peak is formed from the float chiR, and
+  // g_syn * g_syn is a float product; e_peak is stored as float.
+  inline void omega_chi_ref(float ux, float uy, float uz, float ex, float ey, float ez, float bx,
+                            float by, float bz, float B0, float g_syn, float eps, float& e_peak,
+                            float& chiR) {
+    const double gamma  = std::sqrt(1.0 + ux * ux + uy * uy + uz * uz);
+    const double beta_x = ux / gamma, beta_y = uy / gamma, beta_z = uz / gamma;
+    const double bde    = beta_x * ex + beta_y * ey + beta_z * ez;
+    const double cx     = beta_y * bz - beta_z * by;
+    const double cy     = beta_z * bx - beta_x * bz;
+    const double cz     = beta_x * by - beta_y * bx;
+    const double vx = ex + cx, vy = ey + cy, vz = ez + cz;
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    chiR            = static_cast<float>(std::sqrt(v2 - bde * bde) / B0);
+    e_peak          = static_cast<float>(eps * gamma * gamma * chiR / (g_syn * g_syn));
+  }
+
   struct Particles {
     const float *ux, *uy, *uz, *ex, *ey, *ez, *bx, *by, *bz, *w;
   };
@@ -199,11 +217,9 @@ void orc_sync_spectrum_ref32(const float* ux, const float* uy, const float* uz,
   for (std::int64_t p = 0; p < n; ++p) {
     for (std::int64_t e = 0; e < nbins; ++e) {
       const float e_syn = bins[e];
-      double      ep, ch;
-      omega_chi_f64(ux[p], uy[p], uz[p], comp(ex, p), comp(ey, p), comp(ez, p),
-                    bx[p], by[p], bz[p], B0, g_syn, eps, ep, ch);
-      const float e_peak = static_cast<float>(ep);
-      const float chiR   = static_cast<float>(ch);
+      float       e_peak, chiR;
+      omega_chi_ref(ux[p], uy[p], uz[p], comp(ex, p), comp(ey, p), comp(ez, p),
+                    bx[p], by[p], bz[p], B0, g_syn, eps, e_peak, chiR);
       if (e_peak > 0.0) {
         const float F = interp_log_f32(e_syn / e_peak, tx, ty, nt, xmin, xmax, 0.0f);
         float       v = e_syn * chiR * F;
@@ -288,10 +304,9 @@ void orc_sync_spectrum_batched_f64(const float* ux, const float* uy, const float
 // n-1; log-spaced bins add float(1.0/energy), linear bins add 1.  hist_ref32 uses
 // per-thread float duplicates like the reference; hist_f64 sums in double; counts
 // are exact.  Any output pointer may be null.
-static std::size_t energy_bin_index(float ux, float uy, float uz, bool fourvel, float emin,
-                                    float emax, std::size_t n, double& energy) {
-  const float Usqr = ux * ux + uy * uy + uz * uz;
-  energy           = fourvel ? static_cast<double>(std::sqrt(Usqr)) : std::sqrt(1.0 + Usqr);
+static std::size_t energy_bin_index_usqr(float Usqr, bool fourvel, float emin, float emax,
+                                         std::size_t n, double& energy) {
+  energy = fourvel ? static_cast<double>(std::sqrt(Usqr)) : std::sqrt(1.0 + Usqr);
   if (energy < emin) {
     return 0;
   } else if (energy >= emax) {
@@ -301,6 +316,19 @@ static std::size_t energy_bin_index(float ux, float uy, float uz, bool fourvel, 
                                            std::fabs(std::log10(energy / emin)) /
                                            std::log10(emax / emin));
   return ei > n - 1 ? n - 1 : ei;
+}
+
+static std::size_t energy_bin_index(float ux, float uy, float uz, bool fourvel, float emin,
+                                    float emax, std::size_t n, double& energy) {
+  const float Usqr = ux * ux + uy * uy + uz * uz;
+  return energy_bin_index_usqr(Usqr, fourvel, emin, emax, n, energy);
+}
+
+std::int64_t orc_energy_bin_index_usqr(float Usqr, int fourvel, float emin, float emax,
+                                       std::int64_t n) {
+  double energy;
+  return static_cast<std::int64_t>(
+    energy_bin_index_usqr(Usqr, fourvel != 0, emin, emax, static_cast<std::size_t>(n), energy));
 }
 
 std::int64_t orc_energy_bin_index(float ux, float uy, float uz, int fourvel, float emin,

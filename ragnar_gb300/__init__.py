@@ -24,7 +24,7 @@ try:
 except ImportError as exc:  # pragma: no cover - exercised only on a broken install
     raise ImportError(
         "ragnar_gb300's native extension is not built or cannot be loaded "
-        f"({exc}); build it with `python -m ragnar_gb300.build`"
+        f"({exc}); build it with `python ragnar_gb300/build.py`"
     ) from exc
 
 LIBRARY_PATH = os.path.join(_HERE, "_lib", "libragnar_gb300.so")

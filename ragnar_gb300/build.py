@@ -6,7 +6,8 @@
   talks to the library through the C ABI.
 
 Translation units compile in parallel; objects are rebuilt only when a source
-or header is newer.  ``python -m ragnar_gb300.build`` runs it.
+or header is newer.  Run it by path, ``python ragnar_gb300/build.py`` (importing
+the package first would need the extension this script builds).
 """
 
 from __future__ import annotations
