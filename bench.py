@@ -1,0 +1,550 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 synchrotron path.
+
+Workload (one step): the synchrotron spectra of a Tristan-v2 dump-scale particle
+set -- 3 species (e-, e+, p) x 3.3e7 particles = 9.9e7 particles, 512 log photon
+bins 1e-4..1e9 mec^2, FP32 SoA four-velocities with |u| a power law of index -2.2
+on [1, 1e4] times exp(-gamma/3e3) and isotropic directions, magnetic fields with
+log-normal (0, 0.5) magnitude and isotropic directions, weights uniform on
+[0.5, 1.5].  e- and e+ share the scalars B0 = g_syn = e_syn_at_g_syn = 1 and run
+as one batched launch over two segments; protons use e_syn_at_g_syn / 1836.
+Inputs are generated on the device from fixed seeds (synthetic; positions are
+not an input of the spectrum and are not generated).
+
+Reported: evals/s = particles x bins per second (value: device-resident inputs;
+e2e: host-resident pinned inputs through rg_spectrum_run_host, H2D inside the
+timed region), the fused kernel's roofline, the CPU baseline, clocks.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import glob
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "synchrotron particle×bin evals/s, fwd and fwd+adjoint vs plain GPU at 1e-5 rel"
+UNIT = "evals/s"
+NSPECIES = 3
+N_PER_SPECIES = 33_000_000
+NBINS = 512
+BIN_LO, BIN_HI = 1e-4, 1e9
+PROTON_MASS_RATIO = 1836.0
+OPS_PER_EVAL = 6  # IADD, SHF, LOP, LDS.64, FFMA (F), FFMA (accumulate)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of the cpu_baseline sample")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu captures: one 4.19e6-particle species x 512 bins, "
+                         "4 fused-kernel launches, then exit")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------
+# synthetic inputs
+# ---------------------------------------------------------------------------------------
+
+def powerlaw_cutoff_torch(torch, n, gen, device, index=-2.2, lo=1.0, hi=1e4, gcut=3e3):
+    """|u| ~ |u|^index on [lo, hi] times exp(-gamma/gcut), by rejection."""
+    q = index + 1.0
+    out = torch.empty(0, device=device)
+    while out.numel() < n:
+        m = int((n - out.numel()) * 1.1) + 1024
+        r = torch.rand(m, device=device, generator=gen, dtype=torch.float64)
+        u = ((hi**q - lo**q) * r + lo**q) ** (1.0 / q)
+        acc = torch.rand(m, device=device, generator=gen, dtype=torch.float64) < torch.exp(
+            -torch.sqrt(1.0 + u * u) / gcut)
+        out = torch.cat([out, u[acc].float()])
+    return out[:n]
+
+
+def isotropic_torch(torch, mag, gen):
+    n = mag.numel()
+    mu = torch.rand(n, device=mag.device, generator=gen) * 2.0 - 1.0
+    ph = torch.rand(n, device=mag.device, generator=gen) * (2.0 * math.pi)
+    s = torch.sqrt(torch.clamp(1.0 - mu * mu, min=0.0))
+    return [mag * s * torch.cos(ph), mag * s * torch.sin(ph), mag * mu]
+
+
+def make_particles(torch, n_per, nspecies, device, seed):
+    """SoA component tensors (u1..u3, b1..b3, w) holding all species back to back."""
+    comps = [torch.empty(n_per * nspecies, device=device) for _ in range(7)]
+    for s in range(nspecies):
+        gen = torch.Generator(device=device).manual_seed(seed * 101 + s)
+        u = isotropic_torch(torch, powerlaw_cutoff_torch(torch, n_per, gen, device), gen)
+        b = isotropic_torch(torch, torch.exp(0.5 * torch.randn(n_per, device=device, generator=gen)), gen)
+        w = torch.rand(n_per, device=device, generator=gen) + 0.5
+        for k, v in enumerate(u + b + [w]):
+            comps[k][s * n_per:(s + 1) * n_per] = v
+    return comps
+
+
+def make_particles_numpy(n, seed):
+    import numpy as np  # noqa: PLC0415
+
+    rng = np.random.default_rng(seed)
+    q = -1.2
+    out = np.empty(0)
+    while out.size < n:
+        m = int((n - out.size) * 1.1) + 1024
+        u = ((1e4**q - 1.0) * rng.random(m) + 1.0) ** (1.0 / q)
+        out = np.concatenate([out, u[rng.random(m) < np.exp(-np.sqrt(1 + u * u) / 3e3)]])
+    umag = out[:n]
+
+    def iso(mag):
+        mu = rng.uniform(-1, 1, n)
+        ph = rng.uniform(0, 2 * np.pi, n)
+        s = np.sqrt(1 - mu**2)
+        return [(mag * s * np.cos(ph)).astype(np.float32), (mag * s * np.sin(ph)).astype(np.float32),
+                (mag * mu).astype(np.float32)]
+
+    u = iso(umag)
+    b = iso(rng.lognormal(0.0, 0.5, n))
+    # the reference has no per-particle weight: the CPU sample runs with w = 1
+    return {"ux": u[0], "uy": u[1], "uz": u[2], "bx": b[0], "by": b[1], "bz": b[2]}
+
+
+def photon_bins():
+    import numpy as np  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    bins = np.empty(NBINS, np.float32)
+    capi.check(capi.lib().rg_logspace(BIN_LO, BIN_HI, NBINS, bins.ctypes.data))
+    return bins
+
+
+# ---------------------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50", "-i", str(self.gpu)],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        loaded = [r[0] for r in rows if r[2] > 200.0] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# ---------------------------------------------------------------------------------------
+# CPU baseline: the reference's own build when importable, else the oracle port
+# ---------------------------------------------------------------------------------------
+
+def cpu_spectrum_runner():
+    """Returns (kind, fn(P, bins) -> spectrum, threads)."""
+    import oracle  # noqa: PLC0415
+
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    ref_so = glob.glob(os.path.join(ROOT, "oracle", "_ref", "ragnar*.so"))
+    if ref_so:
+        try:
+            import importlib.util  # noqa: PLC0415
+
+            spec = importlib.util.spec_from_file_location("ragnar", ref_so[0])
+            rg = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(rg)
+            rg.Initialize()
+
+            def run_ref(P, bins):
+                prt = rg.Particles_3D("bench")
+                prt.fromArrays({"U1": P["ux"], "U2": P["uy"], "U3": P["uz"],
+                                "B1": P["bx"], "B2": P["by"], "B3": P["bz"]})
+                b = rg.Bins(bins, rg.EnergyUnits.mec2)
+                return rg.SynchrotronSpectrum_3D(prt, b, 1.0, 1.0, 1.0).as_array()
+
+            return "reference", run_ref, threads
+        except Exception:  # noqa: BLE001 - built for another machine
+            pass
+    oracle.build()
+    table = oracle.tabulate_ffunc()
+
+    def run_port(P, bins):
+        return oracle.sync_spectrum_ref32(P, bins, 1.0, 1.0, 1.0, table)
+
+    return "port", run_port, threads
+
+
+def cpu_baseline(target_seconds: float):
+    kind, fn, threads = cpu_spectrum_runner()
+    bins = photon_bins()
+    # calibrate on a small sample, then time one bounded sample of ~target_seconds
+    calib = make_particles_numpy(20000, seed=7)
+    t0 = time.perf_counter()
+    fn(calib, bins)
+    rate = 20000 * NBINS / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(max(rate * target_seconds / NBINS, 20000), 2e7))
+    P = make_particles_numpy(n, seed=8)
+    t0 = time.perf_counter()
+    fn(P, bins)
+    dt = time.perf_counter() - t0
+    return {"value": n * NBINS / dt, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{n} particles of the e- species x {NBINS} bins (one spectrum, {dt:.1f} s)"}
+
+
+def run_reference_arm(args, rank):
+    if rank != 0:
+        return
+    kind, fn, threads = cpu_spectrum_runner()
+    bins = photon_bins()
+    calib = make_particles_numpy(20000, seed=7)
+    t0 = time.perf_counter()
+    fn(calib, bins)
+    rate = 20000 * NBINS / max(time.perf_counter() - t0, 1e-6)
+    per_step = max(90.0 / max(args.steps + args.warmup, 1), 0.2)
+    n = int(min(max(rate * per_step / NBINS, 20000), 2e7))
+    P = make_particles_numpy(n, seed=9)
+    for _ in range(args.warmup):
+        fn(P, bins)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn(P, bins)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = n * NBINS / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy sample of the same workload)",
+        "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"each step: {n} particles of the e- species x {NBINS} bins"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config():
+    return {
+        "workload": "tristan-v2 dump scale: synchrotron spectra of 3 species x 3.3e7 particles, "
+                    "512 log photon bins 1e-4..1e9 mec2",
+        "particles": NSPECIES * N_PER_SPECIES, "photon_bins": NBINS, "species": ["e-", "e+", "p"],
+        "u": "power law -2.2 on [1,1e4] x exp(-gamma/3e3), isotropic",
+        "B": "log-normal(0,0.5) magnitude, isotropic", "weights": "U[0.5,1.5]",
+        "scalars": {"B0": 1.0, "g_syn": 1.0, "e_syn_at_g_syn": {"e-": 1.0, "e+": 1.0, "p": 1 / 1836.0}},
+        "l2": "inputs 2.77 GB per step > 129 MB L2 (no flush needed)",
+        "parallelism": "one rank per GPU, each with its own particle set (weak scaling)",
+    }
+
+
+# ---------------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------------
+
+def traffic_per_particle():
+    """DRAM bytes per particle of the fused kernel from the committed ncu summary."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", open(path).read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np  # noqa: PLC0415
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    dist = world > 1
+    device = torch.device("cuda", local_rank)
+    torch.cuda.set_device(device)
+    capi.check(capi.lib().rg_init(local_rank))
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    stream = torch.cuda.current_stream(device).cuda_stream
+
+    n_per = N_PER_SPECIES
+    comps = make_particles(torch, n_per, NSPECIES, device, seed=1000 + rank)
+    bins = photon_bins()
+    u, b, w = comps[0:3], comps[3:6], comps[6]
+    prt_all = capi.particles(u, b=b, w=w, n=NSPECIES * n_per)
+    off = 2 * n_per
+    prt_p = capi.particles([c[off:] for c in u], b=[c[off:] for c in b], w=w[off:], n=n_per)
+    plan_e = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    plan_p = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0 / PROTON_MASS_RATIO)
+    plan_e.reserve(2)
+    offs_e = torch.tensor([0, n_per, 2 * n_per], dtype=torch.int64, device=device)
+    out_e = torch.empty((2, NBINS), device=device)
+    out_p = torch.empty(NBINS, device=device)
+
+    def step():
+        plan_e.run_batched(prt_all, offs_e, 2, out_e, stream)
+        plan_p.run(prt_p, out_p, stream)
+
+    evals_per_step = NSPECIES * n_per * NBINS
+    launches_per_step = 5  # item prefix + fused + reduce (e+-), fused + reduce (p)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    plan_e.check(stream)
+    plan_p.check(stream)
+    if dist:
+        torch.distributed.barrier()
+    plan_e.enable_timing(True)
+    plan_p.enable_timing(True)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / max(args.steps, 1)
+    ke_ms, ke_n = plan_e.kernel_time()
+    kp_ms, kp_n = plan_p.kernel_time()
+    plan_e.enable_timing(False)
+    plan_p.enable_timing(False)
+    plan_e.check(stream)
+    plan_p.check(stream)
+    spectra_ok = bool(torch.isfinite(out_e).all() and torch.isfinite(out_p).all() and out_e.sum() > 0)
+    if dist:
+        t = torch.tensor([t_step], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+
+    # fused-kernel roofline: FP32-core issue slots (SMs x 128 lanes x clock)
+    kern_ms = (ke_ms + kp_ms) / max(ke_n + kp_n, 1)
+    evals_per_launch = evals_per_step / 2.0
+    achieved = OPS_PER_EVAL * evals_per_launch / (kern_ms / 1e3) / 1e12
+    clk = clocks.get("sm_mhz") or 2070.0
+    peak = sms * 128 * clk * 1e6 / 1e12
+    tpp = traffic_per_particle()
+    roofline = {
+        "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Top/s",
+        "frac": achieved / peak, "kernel": "fused_spectrum_kernel<16>",
+        "kernel_ms_per_launch": kern_ms, "evals_per_launch": evals_per_launch,
+        "peak_basis": f"{sms} SMs x 128 lanes x median SM clock {clk:.0f} MHz sampled during the "
+                      f"timed region (issue slots; no measured FP32 peak is available)",
+        "traffic": None if tpp is None else tpp * evals_per_launch / NBINS,
+    }
+
+    result = {
+        "metric": METRIC, "value": world * evals_per_step / t_step, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, generated on the device)", "config": workload_config(),
+        "roofline": roofline, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+    }
+
+    extra = {"spectra_finite": spectra_ok}
+    # e2e: host-resident pinned inputs through the C ABI, copies inside the timed region
+    if not args.no_e2e:
+        host = [torch.empty(c.numel(), dtype=torch.float32, pin_memory=True) for c in comps]
+        for h, c in zip(host, comps):
+            h.copy_(c)
+        del comps, u, b, w
+        torch.cuda.empty_cache()
+        hout = torch.empty((3, NBINS), dtype=torch.float32, pin_memory=True)
+        dout = torch.empty((3, NBINS), device=device)
+        species = []
+        for s in range(NSPECIES):
+            sl = slice(s * n_per, (s + 1) * n_per)
+            species.append(capi.host_particles([h[sl] for h in host[0:3]], b=[h[sl] for h in host[3:6]],
+                                               w=host[6][sl], n=n_per))
+        plans = [plan_e, plan_e, plan_p]
+
+        def e2e_step():
+            for s in range(NSPECIES):
+                plans[s].run_host(species[s], dout[s], stream)
+            hout.copy_(dout, non_blocking=True)
+            torch.cuda.current_stream(device).synchronize()
+
+        for _ in range(max(args.warmup, 3)):
+            e2e_step()
+        if dist:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        t_e2e = (time.perf_counter() - t0) / max(args.steps, 1)
+        if dist:
+            t = torch.tensor([t_e2e], device=device)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        result["e2e"] = {"value": world * evals_per_step / t_e2e, "unit": UNIT,
+                         "h2d_bytes_per_step": 7 * 4 * NSPECIES * n_per,
+                         "d2h_bytes_per_step": 4 * NSPECIES * NBINS,
+                         "path": "rg_spectrum_run_host (pinned host SoA, chunked H2D overlapped with "
+                                 "the fused kernel) + D2H of the spectra"}
+        plan_e.check(stream)
+        plan_p.check(stream)
+        del host
+
+    # context beside the headline: the plain one-spectrum-per-launch kernel on one
+    # species, and the 1e6-particle x 200-bin configuration (fused and plain)
+    if rank == 0:
+        extra.update(side_measurements(torch, capi, device, stream))
+        if not args.no_cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    result["extra"] = extra
+    plan_e.close()
+    plan_p.close()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def side_measurements(torch, capi, device, stream):
+    import numpy as np  # noqa: PLC0415
+
+    out = {}
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
+
+    n = 8_000_000
+    comps = make_particles(torch, n, 1, device, seed=77)
+    prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
+    bins = photon_bins()
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    o = torch.empty(NBINS, device=device)
+    t_f = timed(lambda: plan.run(prt, o, stream), 10)
+    t_p = timed(lambda: plan.run_plain(prt, o, stream), 2)
+    out["dump_species_8e6_fused_evals_per_s"] = n * NBINS / t_f
+    out["dump_species_8e6_plain_evals_per_s"] = n * NBINS / t_p
+    plan.close()
+    # configuration 1: 1e6 particles, |u| ~ u^-2 on [1,100], B = z, 200 bins 0.01..1e7
+    n1 = 1_000_000
+    gen = torch.Generator(device=device).manual_seed(5)
+    umag = 1.0 / (1.0 - torch.rand(n1, device=device, generator=gen) * (1 - 1e-2))
+    u1 = isotropic_torch(torch, umag, gen)
+    z = torch.zeros(n1, device=device)
+    prt1 = capi.particles(u1, b=[z, z, torch.ones(n1, device=device)], n=n1)
+    b1 = np.empty(200, np.float32)
+    capi.check(capi.lib().rg_logspace(0.01, 1e7, 200, b1.ctypes.data))
+    plan1 = capi.SpectrumPlan(b1, 1.0, 1.0, 1.0)
+    o1 = torch.empty(200, device=device)
+    t1f = timed(lambda: plan1.run(prt1, o1, stream), 20)
+    t1p = timed(lambda: plan1.run_plain(prt1, o1, stream), 5)
+    out["config1_fused_evals_per_s"] = n1 * 200 / t1f
+    out["config1_plain_evals_per_s"] = n1 * 200 / t1p
+    plan1.close()
+    return out
+
+
+def profile_case():
+    """4 launches of the fused spectrum kernel on 2^22 particles x 512 bins
+    (inputs 117 MB + a 256 MB buffer written between launches to flush L2)."""
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    n = 1 << 22
+    comps = make_particles(torch, n, 1, device, seed=3)
+    plan = capi.SpectrumPlan(photon_bins(), 1.0, 1.0, 1.0)
+    out = torch.empty(NBINS, device=device)
+    prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
+    flush = torch.empty(64 << 20, device=device)
+    for _ in range(4):
+        flush.fill_(1.0)
+        plan.run(prt, out, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    plan.check()
+    plan.close()
+    print("profile case done")
+
+
+def main():
+    args = parse_args()
+    if args.profile_case:
+        profile_case()
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+        return
+    if world > 1:
+        import torch  # noqa: PLC0415
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch  # noqa: PLC0415
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

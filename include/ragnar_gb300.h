@@ -79,14 +79,17 @@ int rg_linspace(float start, float stop, int64_t num, float* out);
  * Synchrotron kernel function F(x) = x * int_x^inf K_{5/3}
  * ------------------------------------------------------------------------ */
 
-/* Ffunc_integrand (synchrotron.cpp:28-46) for n device values x -> device y,
- * evaluated on the GPU in FP64 (own K_{5/3} quadrature) with the reference's
- * float rounding steps. */
+/* Ffunc_integrand (synchrotron.cpp:28-46) for n device values x -> device y:
+ * K_{5/3} on the GPU in FP64 (own quadrature), the trapezoid with the reference's
+ * float rounding steps; the 100-point inner grids Logspace(x, 20, 100) are
+ * computed on the host with the platform's log10f/pow as the reference does.
+ * Synchronises `stream`. */
 int rg_ffunc_integrand(const float* x, int64_t n, float* y, void* stream);
 
 /* TabulateFfunc (synchrotron.cpp:48-65): the n-node table on Logspace(xmin, xmax, n)
- * (x nodes computed on the host exactly as Logspace does, y on the GPU in FP64).
- * x and y are device arrays of n floats. */
+ * (x nodes on the host exactly as Logspace does, y as rg_ffunc_integrand with the
+ * x < 1e-6 -> 0 rule).  x and y are device arrays of n floats.  Synchronises
+ * `stream`. */
 int rg_ffunc_table(int64_t n, float xmin, float xmax, float* x, float* y, void* stream);
 
 /* --------------------------------------------------------------------------
@@ -141,6 +144,24 @@ int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* 
  * Extension: the reference computes one spectrum per call. */
 int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p,
                             const int64_t* offsets, int32_t nseg, float* out, void* stream);
+
+/* Host-resident form of rg_spectrum_run: the particle streams in `p` are HOST
+ * pointers (pinned memory gives full copy bandwidth).  They are copied to the
+ * device in chunks on a second stream, overlapped with the fused kernel on
+ * `stream`; the chunk partials are summed in FP64.  `out` is nbins DEVICE
+ * floats.  Replaces the reference's host-mirror + deep_copy ingest followed by
+ * the spectrum (particles.cpp:55-99 then synchrotron.cpp:107-145).  Returns
+ * after enqueueing; the host buffers must stay valid until `stream` completes. */
+int rg_spectrum_run_host(rg_spectrum_plan* plan, const rg_particles* p, float* out,
+                         void* stream);
+
+/* Kernel timing: when enabled, every fused-kernel launch of `plan` is bracketed
+ * by CUDA events on its stream.  rg_spectrum_plan_kernel_time synchronises those
+ * events and returns the summed kernel time (ms) and the launch count since the
+ * last query.  No reference counterpart (the reference has only Kokkos labels,
+ * synchrotron.cpp:131). */
+int rg_spectrum_plan_enable_timing(rg_spectrum_plan* plan, int32_t enable);
+int rg_spectrum_plan_kernel_time(rg_spectrum_plan* plan, double* ms, int64_t* launches);
 
 /* The plain one-spectrum-per-launch kernel (thread per particle, per-eval
  * interpolation as the reference writes it); the baseline the fused kernel is

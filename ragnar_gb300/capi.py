@@ -82,6 +82,9 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_run": [_vp, ctypes.POINTER(Particles), _vp, _vp],
         "rg_spectrum_run_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp],
         "rg_spectrum_run_plain": [_vp, ctypes.POINTER(Particles), _vp, _vp],
+        "rg_spectrum_run_host": [_vp, ctypes.POINTER(Particles), _vp, _vp],
+        "rg_spectrum_plan_enable_timing": [_vp, _i32],
+        "rg_spectrum_plan_kernel_time": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64)],
         "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
         "rg_synchrotron_spectrum_from_dist": [_vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _vp, _vp],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
@@ -134,6 +137,26 @@ def particles(u, b=None, e=None, w=None, n=None) -> Particles:
     return p
 
 
+def host_particles(u, b=None, e=None, w=None, n=None) -> Particles:
+    """rg_particles over HOST arrays (numpy arrays or pinned CPU tensors)."""
+
+    def hp(a):
+        if a is None:
+            return 0
+        if hasattr(a, "data_ptr"):
+            return int(a.data_ptr())
+        return int(a.ctypes.data)
+
+    p = Particles()
+    for d in range(3):
+        p.u[d] = hp(u[d])
+        p.e[d] = hp(e[d]) if e is not None else 0
+        p.b[d] = hp(b[d]) if b is not None else 0
+    p.w = hp(w)
+    p.n = int(n if n is not None else len(u[0]))
+    return p
+
+
 class SpectrumPlan:
     """Owning wrapper of rg_spectrum_plan."""
 
@@ -156,6 +179,20 @@ class SpectrumPlan:
     def run_batched(self, prt: Particles, offsets, nseg: int, out, stream: int = 0) -> None:
         check(lib().rg_spectrum_run_batched(self.handle, ctypes.byref(prt), addr(offsets), nseg,
                                             addr(out), stream))
+
+    def run_host(self, prt: Particles, out, stream: int = 0) -> None:
+        """prt holds HOST pointers (see host_particles)."""
+        check(lib().rg_spectrum_run_host(self.handle, ctypes.byref(prt), addr(out), stream))
+
+    def enable_timing(self, on: bool = True) -> None:
+        check(lib().rg_spectrum_plan_enable_timing(self.handle, int(on)))
+
+    def kernel_time(self) -> tuple[float, int]:
+        """(summed fused-kernel milliseconds, launches) since the last call."""
+        ms = ctypes.c_double()
+        n = _i64()
+        check(lib().rg_spectrum_plan_kernel_time(self.handle, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 
     def reserve(self, nseg: int) -> None:
         check(lib().rg_spectrum_plan_reserve(self.handle, nseg))

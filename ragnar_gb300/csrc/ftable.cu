@@ -56,31 +56,34 @@ namespace rg {
 
   namespace {
 
-    // log10f evaluated as the correctly rounded float of the double log10.
-    __device__ __forceinline__ float log10f_cr(float v) {
-      return __double2float_rn(log10(static_cast<double>(v)));
-    }
+    constexpr int kInner = 100; // inner grid points of Ffunc_integrand (synchrotron.cpp:35)
 
-    // snippets.cpp:48-60 on the device, with the reference's operation order and
-    // no contraction.
-    __device__ float logspace_point_dev(float start, float stop, int num, int i) {
-      if (num == 1) {
-        return start;
+    // Inner grids Logspace(x, 20, 100) of every x in [1e-5, 20], computed on the
+    // host: they are float results of the platform's log10f and pow, exactly as
+    // the reference computes them (log10f is not correctly rounded, so a GPU
+    // evaluation would move some grid points by one ulp).
+    std::vector<float> inner_grids(const std::vector<float>& xs) {
+      std::vector<float> g(xs.size() * kInner, 0.0f);
+      for (std::size_t i = 0; i < xs.size(); ++i) {
+        const float x = xs[i];
+        if (static_cast<double>(x) >= 1e-5 && !(x > 20.0f)) {
+          for (int j = 0; j < kInner; ++j) {
+            g[i * kInner + j] = logspace_point(x, 20.0f, kInner, j);
+          }
+        }
       }
-      const float e = __fadd_rn(log10f_cr(start),
-                                __fdiv_rn(__fmul_rn(static_cast<float>(i),
-                                                    log10f_cr(__fdiv_rn(stop, start))),
-                                          static_cast<float>(num - 1)));
-      return __double2float_rn(pow(10.0, static_cast<double>(e)));
+      return g;
     }
 
     // Ffunc_integrand (synchrotron.cpp:28-46), one warp per x: the lanes evaluate
-    // K_{5/3} on the 100-point inner grid, lane 0 accumulates the trapezoid in the
-    // reference's order (float accumulator, each step through double).
-    __global__ void ffunc_integrand_kernel(const float* __restrict__ x, int64_t n,
+    // K_{5/3} in FP64 on the 100-point inner grid, lane 0 accumulates the
+    // trapezoid in the reference's order (float accumulator, each step through
+    // double).
+    __global__ void ffunc_integrand_kernel(const float* __restrict__ x,
+                                           const float* __restrict__ grids, int64_t n,
                                            float* __restrict__ y, int zero_below_1em6) {
-      __shared__ float xs_s[4][100];
-      __shared__ float ys_s[4][100];
+      __shared__ float xs_s[4][kInner];
+      __shared__ float ys_s[4][kInner];
       const int     wib  = threadIdx.x >> 5;
       const int     lane = threadIdx.x & 31;
       const int64_t i    = static_cast<int64_t>(blockIdx.x) * 4 + wib;
@@ -97,8 +100,8 @@ namespace rg {
       } else if (xi > 20.0f) {
         out = 0.0f;
       } else {
-        for (int j = lane; j < 100; j += 32) {
-          const float xj = logspace_point_dev(xi, 20.0f, 100, j);
+        for (int j = lane; j < kInner; j += 32) {
+          const float xj = grids[i * kInner + j];
           xs_s[wib][j]   = xj;
           ys_s[wib][j]   = __double2float_rn(bessel_k53(static_cast<double>(xj)));
         }
@@ -197,8 +200,15 @@ namespace rg {
     RG_CUDA_TRY(cudaMalloc(&t.d_y, sizeof(float) * n));
     RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float2) * kRefEntries));
     RG_CUDA_TRY(cudaMemcpyAsync(t.d_x, t.h_x.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
-    ffunc_integrand_kernel<<<(n + 3) / 4, 128, 0, s>>>(t.d_x, n, t.d_y, 1);
+    const std::vector<float> grids = inner_grids(t.h_x);
+    float*                   d_grids = nullptr;
+    RG_CUDA_TRY(cudaMalloc(&d_grids, sizeof(float) * grids.size()));
+    RG_CUDA_TRY(cudaMemcpyAsync(d_grids, grids.data(), sizeof(float) * grids.size(),
+                                cudaMemcpyHostToDevice, s));
+    ffunc_integrand_kernel<<<(n + 3) / 4, 128, 0, s>>>(t.d_x, d_grids, n, t.d_y, 1);
     RG_CUDA_TRY(cudaGetLastError());
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    RG_CUDA_TRY(cudaFree(d_grids));
     ref_coef_kernel<<<kRefEntries / 256, 256, 0, s>>>(t.d_x, t.d_y, n, t.ln_xmin, t.dln, t.d_coef);
     RG_CUDA_TRY(cudaGetLastError());
     t.h_y.resize(n);
@@ -228,18 +238,39 @@ namespace rg {
 
 extern "C" {
 
+namespace rg {
+  namespace {
+    // x (device, n) -> y (device, n); `zero_first` applies TabulateFfunc's
+    // x < 1e-6 rule.  Synchronises `s`.
+    int ffunc_eval(const float* x, int64_t n, float* y, int zero_first, cudaStream_t s) {
+      std::vector<float> hx(static_cast<std::size_t>(n));
+      RG_CUDA_TRY(cudaMemcpyAsync(hx.data(), x, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+      RG_CUDA_TRY(cudaStreamSynchronize(s));
+      const std::vector<float> grids = inner_grids(hx);
+      float*                   d_grids = nullptr;
+      RG_CUDA_TRY(cudaMalloc(&d_grids, sizeof(float) * grids.size()));
+      RG_CUDA_TRY(cudaMemcpyAsync(d_grids, grids.data(), sizeof(float) * grids.size(),
+                                  cudaMemcpyHostToDevice, s));
+      ffunc_integrand_kernel<<<static_cast<unsigned>((n + 3) / 4), 128, 0, s>>>(x, d_grids, n, y,
+                                                                               zero_first);
+      const cudaError_t launch = cudaGetLastError();
+      const cudaError_t sync   = cudaStreamSynchronize(s);
+      cudaFree(d_grids);
+      RG_CUDA_TRY(launch);
+      RG_CUDA_TRY(sync);
+      return RG_OK;
+    }
+  } // namespace
+} // namespace rg
+
 int rg_ffunc_integrand(const float* x, int64_t n, float* y, void* stream) {
   if (n <= 0) {
     return RG_OK;
   }
-  const int64_t blocks = (n + 3) / 4;
-  if (blocks > 0x7fffffff) {
+  if ((n + 3) / 4 > 0x7fffffff) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_ffunc_integrand: n too large");
   }
-  rg::ffunc_integrand_kernel<<<static_cast<unsigned>(blocks), 128, 0,
-                               static_cast<cudaStream_t>(stream)>>>(x, n, y, 0);
-  RG_CUDA_TRY(cudaGetLastError());
-  return RG_OK;
+  return rg::ffunc_eval(x, n, y, 0, static_cast<cudaStream_t>(stream));
 }
 
 int rg_ffunc_table(int64_t n, float xmin, float xmax, float* x, float* y, void* stream) {
@@ -250,11 +281,7 @@ int rg_ffunc_table(int64_t n, float xmin, float xmax, float* x, float* y, void* 
   RG_TRY(rg_logspace(xmin, xmax, n, hx.data()));
   auto s = static_cast<cudaStream_t>(stream);
   RG_CUDA_TRY(cudaMemcpyAsync(x, hx.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
-  rg::ffunc_integrand_kernel<<<static_cast<unsigned>((n + 3) / 4), 128, 0, s>>>(x, n, y, 1);
-  RG_CUDA_TRY(cudaGetLastError());
-  // hx must outlive the asynchronous copy
-  RG_CUDA_TRY(cudaStreamSynchronize(s));
-  return RG_OK;
+  return rg::ffunc_eval(x, n, y, 1, s);
 }
 
 // Diagnostics: the FP64 quadratures evaluated on the host (same code as on the GPU).

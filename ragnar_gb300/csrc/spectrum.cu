@@ -494,7 +494,8 @@ namespace rg {
       const float*    ebins;
       const uint8_t*  valid;
       const unsigned* status;
-      float*          out; // nseg x nbins
+      float*          out;   // nseg x nbins
+      double*         acc64; // when set: acc64 += result in FP64 instead of writing out
     };
 
     __global__ void reduce_partials_kernel(const __grid_constant__ ReduceParams r) {
@@ -503,13 +504,13 @@ namespace rg {
       if (bin >= r.nbins) {
         return;
       }
-      float result = 0.0f;
+      double result = 0.0;
       if (*r.status != kDevOk) {
-        result = __int_as_float(0x7fc00000);
+        result = __longlong_as_double(0x7ff8000000000000LL);
       } else {
         const int64_t n_items = total_items(r.item_prefix, r.nseg, r.n_single);
-        const int64_t i0 = items_before(r.item_prefix, s);
-        const int64_t i1 = r.item_prefix ? r.item_prefix[s + 1] : n_items;
+        const int64_t i0      = items_before(r.item_prefix, s);
+        const int64_t i1      = r.item_prefix ? r.item_prefix[s + 1] : n_items;
         if (i1 > i0 && r.valid[bin]) {
           const int b0    = block_of_item(i0, n_items, r.grid);
           const int b1    = block_of_item(i1 - 1, n_items, r.grid);
@@ -518,10 +519,23 @@ namespace rg {
           for (int b = b0; b <= b1; ++b) {
             sum += r.partials[(static_cast<int64_t>(b + s) * r.nslices + slice) * kSliceBins + j];
           }
-          result = __double2float_rn(sum * static_cast<double>(r.ebins[bin]));
+          result = sum * static_cast<double>(r.ebins[bin]);
         }
       }
-      r.out[static_cast<int64_t>(s) * r.nbins + bin] = result;
+      const int64_t o = static_cast<int64_t>(s) * r.nbins + bin;
+      if (r.acc64) {
+        r.acc64[o] += result;
+      } else {
+        r.out[o] = __double2float_rn(result);
+      }
+    }
+
+    __global__ void finalize_acc_kernel(const double* __restrict__ acc, int n,
+                                        const unsigned* status, float* __restrict__ out) {
+      const int i = blockIdx.x * blockDim.x + threadIdx.x;
+      if (i < n) {
+        out[i] = (*status != kDevOk) ? __int_as_float(0x7fc00000) : __double2float_rn(acc[i]);
+      }
     }
 
     // ---- plain baseline kernel ------------------------------------------------------
@@ -692,6 +706,16 @@ struct rg_spectrum_plan {
   int                 prefix_cap  = 0; // segments
   double*             d_plain_acc = nullptr;
   const rg::RefTable* ref         = nullptr;
+  // kernel timing (events bracketing each fused launch)
+  bool                                             timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
+  // host-resident streaming: device staging for two chunks, a copy stream
+  float*       d_stage[2]     = { nullptr, nullptr };
+  int64_t      stage_chunk    = 0;
+  cudaStream_t copy_stream    = nullptr;
+  cudaEvent_t  copied[2]      = { nullptr, nullptr };
+  cudaEvent_t  consumed[2]    = { nullptr, nullptr };
+  double*      d_acc64        = nullptr;
 };
 
 namespace rg {
@@ -802,15 +826,40 @@ namespace rg {
       return RG_OK;
     }
 
+    int timed_launch(rg_spectrum_plan* pl, const FusedParams& fp, dim3 grid, size_t smem,
+                     cudaStream_t s) {
+      std::pair<cudaEvent_t, cudaEvent_t> ev { nullptr, nullptr };
+      if (pl->timing) {
+        if (pl->ev_free.empty()) {
+          RG_CUDA_TRY(cudaEventCreate(&ev.first));
+          RG_CUDA_TRY(cudaEventCreate(&ev.second));
+        } else {
+          ev = pl->ev_free.back();
+          pl->ev_free.pop_back();
+        }
+        RG_CUDA_TRY(cudaEventRecord(ev.first, s));
+      }
+      RG_CUDA_TRY(launch_fused(pl->K, fp, grid, smem, s));
+      if (pl->timing) {
+        RG_CUDA_TRY(cudaEventRecord(ev.second, s));
+        pl->ev_used.push_back(ev);
+      }
+      return RG_OK;
+    }
+
     // Launches fused + reduce.  `d_off` (device, nseg + 1) may be null for a
-    // single segment [0, n_single).
+    // single segment [0, n_single).  With `acc64` the spectra are added in FP64
+    // to acc64 (nseg x nbins) instead of being written to `out`.
     int run_fused(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off,
-                  int64_t n_single, int nseg, float* out, cudaStream_t s) {
+                  int64_t n_single, int nseg, float* out, cudaStream_t s,
+                  double* acc64 = nullptr) {
       if (nseg <= 0 || pl->nbins == 0) {
         return RG_OK;
       }
       if (pl->zero) {
-        RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins * nseg, s));
+        if (!acc64) {
+          RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins * nseg, s));
+        }
         return RG_OK;
       }
       RG_TRY(plan_reserve(pl, nseg));
@@ -860,7 +909,7 @@ namespace rg {
       }
       const bool any = d_off ? true : n_single > 0;
       if (any) {
-        RG_CUDA_TRY(launch_fused(pl->K, fp, dim3(G, pl->nslices), fused_smem(nslots), s));
+        RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(nslots), s));
       }
       ReduceParams rp {};
       rp.partials    = pl->d_partials;
@@ -874,6 +923,7 @@ namespace rg {
       rp.valid       = pl->d_valid;
       rp.status      = pl->d_status;
       rp.out         = out;
+      rp.acc64       = acc64;
       dim3 rgrid((pl->nbins + 127) / 128, nseg);
       reduce_partials_kernel<<<rgrid, 128, 0, s>>>(rp);
       RG_CUDA_TRY(cudaGetLastError());
@@ -962,7 +1012,102 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_partials);
   cudaFree(pl->d_prefix);
   cudaFree(pl->d_plain_acc);
+  cudaFree(pl->d_stage[0]);
+  cudaFree(pl->d_stage[1]);
+  cudaFree(pl->d_acc64);
+  for (int b = 0; b < 2; ++b) {
+    if (pl->copied[b]) cudaEventDestroy(pl->copied[b]);
+    if (pl->consumed[b]) cudaEventDestroy(pl->consumed[b]);
+  }
+  if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
+  for (auto* v : { &pl->ev_used, &pl->ev_free }) {
+    for (auto& e : *v) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+  }
   delete pl;
+  return RG_OK;
+}
+
+int rg_spectrum_plan_enable_timing(rg_spectrum_plan* pl, int32_t enable) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  pl->timing = enable != 0;
+  return RG_OK;
+}
+
+int rg_spectrum_plan_kernel_time(rg_spectrum_plan* pl, double* ms, int64_t* launches) {
+  if (!pl || !ms) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_kernel_time: bad arguments");
+  }
+  double total = 0.0;
+  if (!pl->ev_used.empty()) {
+    RG_CUDA_TRY(cudaEventSynchronize(pl->ev_used.back().second));
+  }
+  for (auto& e : pl->ev_used) {
+    float t = 0.0f;
+    RG_CUDA_TRY(cudaEventElapsedTime(&t, e.first, e.second));
+    total += t;
+  }
+  if (launches) {
+    *launches = static_cast<int64_t>(pl->ev_used.size());
+  }
+  pl->ev_free.insert(pl->ev_free.end(), pl->ev_used.begin(), pl->ev_used.end());
+  pl->ev_used.clear();
+  *ms = total;
+  return RG_OK;
+}
+
+int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out, void* stream) {
+  if (!pl || (!out && pl->nbins > 0) || pl->source != rg::kSrcParticles) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_host: bad arguments");
+  }
+  RG_TRY(rg::check_particles(p));
+  if (pl->nbins == 0) {
+    return RG_OK;
+  }
+  auto s = static_cast<cudaStream_t>(stream);
+  constexpr int64_t kStageChunk = int64_t(1) << 22; // particles per staged chunk
+  if (!pl->d_stage[0]) {
+    for (int b = 0; b < 2; ++b) {
+      RG_CUDA_TRY(cudaMalloc(&pl->d_stage[b], sizeof(float) * rg::kComps * kStageChunk));
+      RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->copied[b], cudaEventDisableTiming));
+      RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->consumed[b], cudaEventDisableTiming));
+    }
+    RG_CUDA_TRY(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
+    RG_CUDA_TRY(cudaMalloc(&pl->d_acc64, sizeof(double) * pl->nbins));
+    pl->stage_chunk = kStageChunk;
+  }
+  const float* host[rg::kComps];
+  rg::particle_comps(p, host);
+  RG_CUDA_TRY(cudaMemsetAsync(pl->d_acc64, 0, sizeof(double) * pl->nbins, s));
+  // staging may still be read by earlier work on `s`
+  RG_CUDA_TRY(cudaEventRecord(pl->consumed[0], s));
+  RG_CUDA_TRY(cudaEventRecord(pl->consumed[1], s));
+  const int64_t n = p->n;
+  for (int64_t c = 0, a = 0; a < n; ++c, a += kStageChunk) {
+    const int     b = static_cast<int>(c & 1);
+    const int64_t m = std::min(kStageChunk, n - a);
+    RG_CUDA_TRY(cudaStreamWaitEvent(pl->copy_stream, pl->consumed[b], 0));
+    const float* dev[rg::kComps] = {};
+    for (int k = 0; k < rg::kComps; ++k) {
+      if (host[k]) {
+        float* dst = pl->d_stage[b] + k * kStageChunk;
+        RG_CUDA_TRY(cudaMemcpyAsync(dst, host[k] + a, sizeof(float) * m, cudaMemcpyHostToDevice,
+                                    pl->copy_stream));
+        dev[k] = dst;
+      }
+    }
+    RG_CUDA_TRY(cudaEventRecord(pl->copied[b], pl->copy_stream));
+    RG_CUDA_TRY(cudaStreamWaitEvent(s, pl->copied[b], 0));
+    RG_TRY(rg::run_fused(pl, dev, nullptr, m, 1, out, s, pl->d_acc64));
+    RG_CUDA_TRY(cudaEventRecord(pl->consumed[b], s));
+  }
+  rg::finalize_acc_kernel<<<(pl->nbins + 255) / 256, 256, 0, s>>>(pl->d_acc64, pl->nbins,
+                                                                  pl->d_status, out);
+  RG_CUDA_TRY(cudaGetLastError());
   return RG_OK;
 }
 

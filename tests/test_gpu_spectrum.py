@@ -1,0 +1,223 @@
+"""GPU parity of the particle spectrum, called through the C ABI.
+
+The fused kernel is compared with the oracle's FP64 ground truth (1e-5 relative
+on bins above 1e-12 of the peak) and with the reference's own outputs (golden
+fixtures), on the reference's edge cases: empty and tiny inputs, sizes around
+the chunk and warp boundaries, bins that are not log-spaced or not positive,
+particles with no emission (u = 0, u parallel to B), E fields, weights,
+unaligned streams; plus the batched launch and size-independent properties at
+full size (additivity over segments, exact power-of-two scaling, bit-identical
+reruns).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import SPECTRUM_RTOL, golden, max_rel, particles
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+capi = pytest.importorskip("ragnar_gb300.capi")
+
+
+def to_device(P, dev):
+    T = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in P.items()}
+    prt = capi.particles([T["ux"], T["uy"], T["uz"]],
+                         b=[T.get("bx"), T.get("by"), T.get("bz")],
+                         e=[T.get("ex"), T.get("ey"), T.get("ez")] if "ex" in T else None,
+                         w=T.get("w"), n=len(P["ux"]))
+    return T, prt
+
+
+def gpu_spectrum(P, bins, dev, B0=1.0, g=1.0, eps=1.0, plain=False):
+    T, prt = to_device(P, dev)
+    plan = capi.SpectrumPlan(bins, B0, g, eps)
+    out = torch.full((len(bins),), -1.0, device=dev)
+    (plan.run_plain if plain else plan.run)(prt, out)
+    plan.check()
+    res = out.cpu().numpy()
+    plan.close()
+    return res
+
+
+@pytest.fixture(scope="module")
+def table(oracle_lib):
+    return oracle_lib.tabulate_ffunc()
+
+
+@pytest.mark.parametrize("case", ["c1", "iso", "efield"])
+def test_matches_reference_fixtures(gpu, oracle_lib, table, case):
+    g = golden("spectrum")
+    u, b, e = g[f"{case}_u"], g[f"{case}_b"], g[f"{case}_e"]
+    P = {"ux": u[0], "uy": u[1], "uz": u[2], "bx": b[0], "by": b[1], "bz": b[2]}
+    if np.any(e != 0):
+        P.update(ex=e[0], ey=e[1], ez=e[2])
+    bins, ref = g[f"{case}_bins"], g[f"{case}_ref"]
+    got = gpu_spectrum(P, bins, gpu)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)
+    assert max_rel(got, truth) <= SPECTRUM_RTOL
+    # vs the reference itself: GPU error plus the reference's own FP32 error
+    assert max_rel(got, ref) <= SPECTRUM_RTOL + max_rel(ref, truth)
+    assert np.array_equal(got == 0, ref == 0)
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 4, 5, 511, 512, 513, 1025, 4099])
+@pytest.mark.parametrize("nbins", [1, 31, 32, 33, 200])
+def test_sizes_and_edges(gpu, oracle_lib, table, n, nbins):
+    P = particles(max(n, 1), seed=n * 7 + nbins, bfield="iso")
+    if n == 0:
+        P = {k: v[:0] for k, v in P.items()}
+    bins = oracle_lib.logspace(0.01, 1e7, nbins) if nbins > 1 else np.array([3.0], np.float32)
+    got = gpu_spectrum(P, bins, gpu)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table) if n else np.zeros(nbins)
+    assert got.shape == (nbins,)
+    assert max_rel(got, truth) <= SPECTRUM_RTOL
+    assert np.all(got[truth == 0] == 0)
+
+
+@pytest.mark.parametrize("nbins,lo,hi", [(512, 1e-4, 1e9), (513, 1e-4, 1e9), (1024, 1e-2, 1e13),
+                                          (1500, 1e-3, 1e8)])
+def test_many_bins_and_slices(gpu, oracle_lib, table, nbins, lo, hi):
+    P = particles(20000, seed=nbins, bfield="iso", weights=True, umax=1e4, index=-2.2)
+    bins = oracle_lib.logspace(lo, hi, nbins)
+    got = gpu_spectrum(P, bins, gpu)
+    assert max_rel(got, oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)) <= SPECTRUM_RTOL
+
+
+def test_linear_and_nonpositive_bins(gpu, oracle_lib, table):
+    P = particles(5000, seed=3, bfield="iso")
+    bins = oracle_lib.linspace(-5.0, 300.0, 250)  # includes negative and zero-crossing bins
+    got = gpu_spectrum(P, bins, gpu)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)
+    assert np.all(got[bins <= 0] == 0)
+    assert max_rel(got, truth) <= SPECTRUM_RTOL
+
+
+def test_non_emitting_particles(gpu, oracle_lib, table):
+    n = 3000
+    P = particles(n, seed=5)
+    P["ux"][:1000] = 0.0  # at rest: chiR = 0 without E
+    P["uy"][:1000] = 0.0
+    P["uz"][:1000] = 0.0
+    P["ux"][1000:2000] = 0.0  # moving along B: u x B = 0
+    P["uy"][1000:2000] = 0.0
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    got = gpu_spectrum(P, bins, gpu)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)
+    only = oracle_lib.sync_spectrum_f64({k: v[2000:] for k, v in P.items()}, bins, 1.0, 1.0, 1.0, table)
+    np.testing.assert_allclose(truth, only, rtol=1e-12)
+    assert max_rel(got, truth) <= SPECTRUM_RTOL
+
+
+@pytest.mark.parametrize("B0,g,eps", [(0.5, 2.0, 3.0), (3.0, 0.7, 137 * 27 / 8 * 0.1), (1.0, 1.0, -1.0)])
+def test_scalars(gpu, oracle_lib, table, B0, g, eps):
+    P = particles(4000, seed=11, bfield="iso", efield=True, weights=True)
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    got = gpu_spectrum(P, bins, gpu, B0, g, eps)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, B0, g, eps, table)
+    if eps < 0:  # e_peak < 0 for every particle: the reference adds nothing
+        assert np.all(got == 0) and np.all(truth == 0)
+    else:
+        assert max_rel(got, truth) <= SPECTRUM_RTOL
+
+
+def test_unaligned_streams_take_plain_loads(gpu, oracle_lib, table):
+    P = particles(10001, seed=2, bfield="iso", weights=True)
+    T = {k: torch.from_numpy(np.concatenate([[0.0], v]).astype(np.float32)).to(gpu) for k, v in P.items()}
+    # views starting one float in: 4-byte aligned, not 16-byte aligned
+    prt = capi.particles([T["ux"][1:], T["uy"][1:], T["uz"][1:]], b=[T["bx"][1:], T["by"][1:], T["bz"][1:]],
+                         w=T["w"][1:], n=10001)
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    out = torch.empty(200, device=gpu)
+    plan.run(prt, out)
+    plan.check()
+    assert max_rel(out.cpu().numpy(), oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)) <= SPECTRUM_RTOL
+
+
+def test_plain_kernel(gpu, oracle_lib, table):
+    P = particles(30000, seed=4, bfield="iso", weights=True)
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    got = gpu_spectrum(P, bins, gpu, plain=True)
+    # FP32 kinematics and log10f interpolation per eval, as the reference writes them
+    assert max_rel(got, oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)) < 2e-4
+
+
+def test_batched_segments(gpu, oracle_lib, table):
+    P = particles(60000, seed=8, bfield="iso", weights=True)
+    offs = np.array([0, 0, 1, 100, 100, 513, 5000, 20000, 20003, 60000], np.int64)
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    T, prt = to_device(P, gpu)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    nseg = len(offs) - 1
+    plan.reserve(nseg)
+    out = torch.empty((nseg, 200), device=gpu)
+    plan.run_batched(prt, torch.from_numpy(offs).to(gpu), nseg, out)
+    plan.check()
+    got = out.cpu().numpy()
+    truth = oracle_lib.sync_spectrum_batched_f64(P, offs, bins, 1.0, 1.0, 1.0, table)
+    for s in range(nseg):
+        if offs[s + 1] == offs[s]:
+            assert np.all(got[s] == 0)
+        else:
+            assert max_rel(got[s], truth[s]) <= SPECTRUM_RTOL, s
+
+
+def test_batched_rejects_bad_offsets(gpu, oracle_lib):
+    P = particles(1000, seed=1)
+    T, prt = to_device(P, gpu)
+    plan = capi.SpectrumPlan(oracle_lib.logspace(0.01, 1e7, 64), 1.0, 1.0, 1.0)
+    plan.reserve(3)
+    out = torch.empty((3, 64), device=gpu)
+    for offs in ([0, 500, 400, 1000], [0, 10, 20, 1001]):
+        plan.run_batched(prt, torch.tensor(offs, dtype=torch.int64, device=gpu), 3, out)
+        with pytest.raises(capi.RgError, match="offsets"):
+            plan.check()
+    # the plan is usable again after the failure was reported
+    plan.run_batched(prt, torch.tensor([0, 10, 20, 1000], dtype=torch.int64, device=gpu), 3, out)
+    plan.check()
+    assert torch.isfinite(out).all()
+
+
+def test_full_size_properties(gpu):
+    """Config-2 scale (1e8 particles, 512 bins): additivity over a batched split,
+    exact scaling by powers of two, bit-identical reruns."""
+    n = 100_000_000
+    gen = torch.Generator(device=gpu).manual_seed(0)
+
+    def iso(mag):
+        mu = torch.rand(n, device=gpu, generator=gen) * 2 - 1
+        ph = torch.rand(n, device=gpu, generator=gen) * (2 * np.pi)
+        s = torch.sqrt(1 - mu * mu)
+        return [mag * s * torch.cos(ph), mag * s * torch.sin(ph), mag * mu]
+
+    umag = 1.0 / (1.0 - torch.rand(n, device=gpu, generator=gen) * (1 - 1e-4))
+    u = iso(umag)
+    b = iso(torch.exp(0.5 * torch.randn(n, device=gpu, generator=gen)))
+    w = torch.rand(n, device=gpu, generator=gen) + 0.5
+    bins = np.logspace(-4, 9, 512).astype(np.float32)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    plan.reserve(2)
+    prt = capi.particles(u, b=b, w=w, n=n)
+    full = torch.empty(512, device=gpu)
+    plan.run(prt, full)
+    plan.check()
+    again = torch.empty(512, device=gpu)
+    plan.run(prt, again)
+    plan.check()
+    assert torch.equal(full, again)
+    split = torch.empty((2, 512), device=gpu)
+    offs = torch.tensor([0, 37_000_001, n], dtype=torch.int64, device=gpu)
+    plan.run_batched(prt, offs, 2, split)
+    plan.check()
+    f, s = full.double().cpu().numpy(), split.double().sum(0).cpu().numpy()
+    assert max_rel(s, f) < 1e-6
+    w2 = w * 2.0
+    prt2 = capi.particles(u, b=b, w=w2, n=n)
+    doubled = torch.empty(512, device=gpu)
+    plan.run(prt2, doubled)
+    plan.check()
+    assert torch.equal(doubled, full * 2)
