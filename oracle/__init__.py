@@ -67,6 +67,14 @@ def _declare(L: ctypes.CDLL) -> None:
     fd = [_f32p, _f32p, _i64, _i64, _int, _f32p, _i64, _f32, _f32, _f32p, _f32p, _i64]
     L.orc_sync_from_dist_ref32.argtypes = fd + [_f32p, _int]
     L.orc_sync_from_dist_f64.argtypes = fd + [_f64p, _int]
+    _d = ctypes.c_double
+    L.orc_smooth_coefficients.argtypes = [_i64, _d, _d, _f64p, _int]
+    L.orc_exact_F.argtypes = [_d]
+    L.orc_exact_F.restype = _d
+    D10 = [_f64p] * 10
+    sm = [_i64, _f32p, _i64, _d, _d, _d, _f32p, _i64, _d, _d]
+    L.orc_sync_smooth_f64.argtypes = D10 + sm + [_f64p, _int]
+    L.orc_sync_smooth_grad_f64.argtypes = D10 + sm + [_f64p, _f64p, _f64p, _f64p, _f64p, _int]
 
 
 def _p(a, ptype=_f32p):
@@ -198,3 +206,58 @@ def sync_from_dist_f64(gb, f, log_spaced, bins, g_syn, eps, table, nthreads=0):
                                  _p(bins), len(bins), g_syn, eps, _p(tx), _p(ty), len(tx),
                                  _p(out, _f64p), nthreads)
     return out
+
+
+# ---- differentiable (smooth) mode ---------------------------------------------------
+
+SMOOTH_XMIN, SMOOTH_XMAX = 1e-6, 100.0
+
+
+def exact_F(x: float) -> float:
+    """x int_x^inf K_{5/3}, FP64 from std::cyl_bessel_k."""
+    return float(lib().orc_exact_F(x))
+
+
+def smooth_coefficients(nseg: int, xmin: float = SMOOTH_XMIN, xmax: float = SMOOTH_XMAX,
+                        nthreads=0) -> np.ndarray:
+    """Hermite segment coefficients [nseg, 4] in FP64."""
+    out = np.empty((nseg, 4), np.float64)
+    lib().orc_smooth_coefficients(nseg, xmin, xmax, _p(out, _f64p), nthreads)
+    return out
+
+
+def _f64arr(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _smooth_args(prt, bins, coef, xmin, xmax):
+    keys = ("ux", "uy", "uz", "ex", "ey", "ez", "bx", "by", "bz", "w")
+    arrs = [_f64arr(prt.get(k)) for k in keys]
+    coef = np.ascontiguousarray(coef, dtype=np.float32)
+    nseg = coef.shape[0]
+    ln_xmin = float(np.log(xmin))
+    dln = float(np.log(xmax / xmin) / nseg)
+    return arrs, len(arrs[0]), _f32arr(bins), coef, nseg, ln_xmin, dln
+
+
+def sync_smooth_f64(prt: dict, bins, B0, g_syn, eps, coef, xmin=SMOOTH_XMIN, xmax=SMOOTH_XMAX,
+                    nthreads=0) -> np.ndarray:
+    """Smooth-mode spectrum in FP64 (particle data taken as float64)."""
+    arrs, n, bins, coef, nseg, lnx, dln = _smooth_args(prt, bins, coef, xmin, xmax)
+    out = np.empty(len(bins), np.float64)
+    lib().orc_sync_smooth_f64(*[_p(a, _f64p) for a in arrs], n, _p(bins), len(bins), B0, g_syn, eps,
+                              _p(coef), nseg, lnx, dln, _p(out, _f64p), nthreads)
+    return out
+
+
+def sync_smooth_grad_f64(prt: dict, bins, B0, g_syn, eps, coef, gS, xmin=SMOOTH_XMIN,
+                         xmax=SMOOTH_XMAX, nthreads=0):
+    """(dL/dw, dL/du [3, n]) of the smooth-mode spectrum given gS = dL/dS."""
+    arrs, n, bins, coef, nseg, lnx, dln = _smooth_args(prt, bins, coef, xmin, xmax)
+    gS = _f64arr(gS)
+    gw = np.empty(n, np.float64)
+    gu = np.empty((3, n), np.float64)
+    lib().orc_sync_smooth_grad_f64(*[_p(a, _f64p) for a in arrs], n, _p(bins), len(bins), B0, g_syn,
+                                   eps, _p(coef), nseg, lnx, dln, _p(gS, _f64p), _p(gw, _f64p),
+                                   _p(gu[0], _f64p), _p(gu[1], _f64p), _p(gu[2], _f64p), nthreads)
+    return gw, gu

@@ -461,4 +461,231 @@ void orc_sync_from_dist_f64(const float* gb, const float* f, std::int64_t ng,
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Differentiable ("smooth") mode.  F on [xmin, xmax) is the C1 cubic Hermite
+// interpolant in t = (ln x - ln xmin)/dln through nodes x_j = xmin e^{j dln} with
+// values F(x_j) = x_j int_{x_j}^inf K_{5/3} and slopes dF/dln x = F - x^2 K_{5/3}(x)
+// (so F'(x) = F/x - x K_{5/3}); zero outside, like the reference table's support.
+// Segment j in tau = t - j: F = c0 + tau (c1 + tau (c2 + tau c3)).
+// ---------------------------------------------------------------------------------
+
+namespace {
+
+  // Gauss-Legendre nodes/weights on [-1, 1] (Newton on P_n).
+  void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+      double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+      for (int it = 0; it < 100; ++it) {
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; ++k) {
+          const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+          p0              = p1;
+          p1              = p2;
+        }
+        const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+        const double dz = p1 / dp;
+        z -= dz;
+        if (std::fabs(dz) < 1e-16) {
+          break;
+        }
+      }
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0              = p1;
+        p1              = p2;
+      }
+      const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+      x[i]            = z;
+      w[i]            = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+  }
+
+  // F(x) = x int_x^inf K_{5/3}(t) dt with t = x e^v (dt = t dv), v in [0, ln(60/x)],
+  // 96 panels x 16-point Gauss-Legendre, K from std::cyl_bessel_k.
+  double exact_F_oracle(double x) {
+    static std::vector<double> gx, gw;
+    if (gx.empty()) {
+      gauss_legendre(16, gx, gw);
+    }
+    const double V = std::log(std::max(60.0, 2.0 * x) / x) + 1.0;
+    const int    P = 96;
+    double       s = 0.0;
+    for (int p = 0; p < P; ++p) {
+      const double a = V * p / P, b = V * (p + 1) / P, h = 0.5 * (b - a), c = 0.5 * (a + b);
+      for (int i = 0; i < 16; ++i) {
+        const double v = c + h * gx[i];
+        const double t = x * std::exp(v);
+        s += gw[i] * h * t * std::cyl_bessel_k(kFiveThird, t);
+      }
+    }
+    return x * s;
+  }
+
+  struct SmoothTable {
+    const float* c; // nseg x 4
+    int64_t      nseg;
+    double       ln_xmin, dln;
+  };
+
+  // F and dF/dln x of the Hermite interpolant at ln x (0 outside the support).
+  inline void smooth_eval(const SmoothTable& T, double lnx, double& F, double& dF) {
+    const double t = (lnx - T.ln_xmin) / T.dln;
+    F = dF = 0.0;
+    if (!(t >= 0.0) || !(t < static_cast<double>(T.nseg))) {
+      return;
+    }
+    const int64_t j   = static_cast<int64_t>(t);
+    const double  tau = t - static_cast<double>(j);
+    const double  c0 = T.c[4 * j], c1 = T.c[4 * j + 1], c2 = T.c[4 * j + 2], c3 = T.c[4 * j + 3];
+    F  = c0 + tau * (c1 + tau * (c2 + tau * c3));
+    dF = (c1 + tau * (2.0 * c2 + 3.0 * tau * c3)) / T.dln;
+  }
+
+  // chi_R, e_peak and their u-gradients (d ln chi / du, d ln e_peak / du) in double.
+  struct Kin {
+    double chi, lneps;
+    double dlnchi[3], dlneps[3];
+  };
+
+  inline bool kinematics(const double u[3], const double E[3], const double B[3], double B0,
+                         double g_syn, double eps, Kin& k) {
+    const double G     = 1.0 + u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const double gamma = std::sqrt(G);
+    const double c[3]  = { u[1] * B[2] - u[2] * B[1], u[2] * B[0] - u[0] * B[2],
+                           u[0] * B[1] - u[1] * B[0] };
+    const double V[3]  = { gamma * E[0] + c[0], gamma * E[1] + c[1], gamma * E[2] + c[2] };
+    const double uE    = u[0] * E[0] + u[1] * E[1] + u[2] * E[2];
+    const double W     = V[0] * V[0] + V[1] * V[1] + V[2] * V[2] - uE * uE;
+    const double K0    = eps / (g_syn * g_syn * B0);
+    if (!(W > 0.0) || !(K0 > 0.0)) {
+      return false;
+    }
+    k.chi   = std::sqrt(W) / (gamma * B0);
+    k.lneps = std::log(K0) + 0.5 * std::log(G) + 0.5 * std::log(W);
+    // dW/du = (2 V.E / gamma) u + 2 B x V - 2 (u.E) E
+    const double VE     = V[0] * E[0] + V[1] * E[1] + V[2] * E[2];
+    const double BxV[3] = { B[1] * V[2] - B[2] * V[1], B[2] * V[0] - B[0] * V[2],
+                            B[0] * V[1] - B[1] * V[0] };
+    for (int d = 0; d < 3; ++d) {
+      const double gW  = 2.0 * VE / gamma * u[d] + 2.0 * BxV[d] - 2.0 * uE * E[d];
+      const double glG = 2.0 * u[d] / G;
+      k.dlnchi[d]      = 0.5 * gW / W - 0.5 * glG;
+      k.dlneps[d]      = 0.5 * glG + 0.5 * gW / W;
+    }
+    return true;
+  }
+
+  inline double dcomp(const double* p, std::int64_t i) {
+    return p ? p[i] : 0.0;
+  }
+
+} // namespace
+
+// Coefficients of the smooth table (nseg segments on [xmin, xmax)) in FP64 from
+// std::cyl_bessel_k; coef is [nseg x 4].
+void orc_smooth_coefficients(std::int64_t nseg, double xmin, double xmax, double* coef,
+                             int nthreads) {
+  const double        ln_xmin = std::log(xmin), dln = std::log(xmax / xmin) / nseg;
+  std::vector<double> F(nseg + 1), D(nseg + 1);
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads_or_default(nthreads))
+  for (std::int64_t j = 0; j <= nseg; ++j) {
+    const double x = std::exp(ln_xmin + j * dln);
+    F[j]           = exact_F_oracle(x);
+    D[j]           = F[j] - x * x * std::cyl_bessel_k(kFiveThird, x);
+  }
+  for (std::int64_t j = 0; j < nseg; ++j) {
+    coef[4 * j]     = F[j];
+    coef[4 * j + 1] = D[j] * dln;
+    coef[4 * j + 2] = 3.0 * (F[j + 1] - F[j]) - dln * (2.0 * D[j] + D[j + 1]);
+    coef[4 * j + 3] = 2.0 * (F[j] - F[j + 1]) + dln * (D[j] + D[j + 1]);
+  }
+}
+
+double orc_exact_F(double x) {
+  return exact_F_oracle(x);
+}
+
+// Smooth-mode spectrum S[b] = e_b sum_p w_p chi_p F(e_b / e_peak_p) in FP64 for
+// double particle data (any component pointer may be null = 0; w null = 1).
+void orc_sync_smooth_f64(const double* ux, const double* uy, const double* uz, const double* ex,
+                         const double* ey, const double* ez, const double* bx, const double* by,
+                         const double* bz, const double* w, std::int64_t n, const float* bins,
+                         std::int64_t nbins, double B0, double g_syn, double eps, const float* coef,
+                         std::int64_t nseg, double ln_xmin, double dln, double* out, int nthreads) {
+  const int           nth = threads_or_default(nthreads);
+  const SmoothTable   T { coef, nseg, ln_xmin, dln };
+  std::vector<double> dup(static_cast<std::size_t>(nth) * nbins, 0.0);
+#pragma omp parallel num_threads(nth)
+  {
+    double* acc = dup.data() + static_cast<std::size_t>(omp_get_thread_num()) * nbins;
+#pragma omp for schedule(static)
+    for (std::int64_t p = 0; p < n; ++p) {
+      const double u[3] = { ux[p], uy[p], uz[p] };
+      const double E[3] = { dcomp(ex, p), dcomp(ey, p), dcomp(ez, p) };
+      const double B[3] = { dcomp(bx, p), dcomp(by, p), dcomp(bz, p) };
+      Kin          k;
+      if (!kinematics(u, E, B, B0, g_syn, eps, k)) {
+        continue;
+      }
+      const double amp = k.chi * (w ? w[p] : 1.0);
+      for (std::int64_t b = 0; b < nbins; ++b) {
+        double F, dF;
+        smooth_eval(T, std::log(static_cast<double>(bins[b])) - k.lneps, F, dF);
+        acc[b] += static_cast<double>(bins[b]) * amp * F;
+      }
+    }
+  }
+  for (std::int64_t b = 0; b < nbins; ++b) {
+    double s = 0.0;
+    for (int t = 0; t < nth; ++t) {
+      s += dup[static_cast<std::size_t>(t) * nbins + b];
+    }
+    out[b] = s;
+  }
+}
+
+// Analytic gradient of L(S) given gS = dL/dS (nbins): dL/dw_p and dL/du_p of the
+// smooth-mode spectrum, in FP64.  gw / gu* may be null.
+void orc_sync_smooth_grad_f64(const double* ux, const double* uy, const double* uz,
+                              const double* ex, const double* ey, const double* ez,
+                              const double* bx, const double* by, const double* bz,
+                              const double* w, std::int64_t n, const float* bins,
+                              std::int64_t nbins, double B0, double g_syn, double eps,
+                              const float* coef, std::int64_t nseg, double ln_xmin, double dln,
+                              const double* gS, double* gw, double* gux, double* guy, double* guz,
+                              int nthreads) {
+  const SmoothTable T { coef, nseg, ln_xmin, dln };
+#pragma omp parallel for schedule(static) num_threads(threads_or_default(nthreads))
+  for (std::int64_t p = 0; p < n; ++p) {
+    const double u[3] = { ux[p], uy[p], uz[p] };
+    const double E[3] = { dcomp(ex, p), dcomp(ey, p), dcomp(ez, p) };
+    const double B[3] = { dcomp(bx, p), dcomp(by, p), dcomp(bz, p) };
+    Kin          k;
+    double       g[3] = { 0.0, 0.0, 0.0 }, gwp = 0.0;
+    if (kinematics(u, E, B, B0, g_syn, eps, k)) {
+      double R1 = 0.0, R2 = 0.0;
+      for (std::int64_t b = 0; b < nbins; ++b) {
+        double F, dF;
+        smooth_eval(T, std::log(static_cast<double>(bins[b])) - k.lneps, F, dF);
+        const double ge = gS[b] * static_cast<double>(bins[b]);
+        R1 += ge * F;
+        R2 += ge * dF;
+      }
+      const double wp  = w ? w[p] : 1.0;
+      const double amp = k.chi * wp;
+      gwp              = k.chi * R1;
+      for (int d = 0; d < 3; ++d) {
+        g[d] = amp * (R1 * k.dlnchi[d] - R2 * k.dlneps[d]);
+      }
+    }
+    if (gw) gw[p] = gwp;
+    if (gux) gux[p] = g[0];
+    if (guy) guy[p] = g[1];
+    if (guz) guz[p] = g[2];
+  }
+}
+
 } // extern "C"

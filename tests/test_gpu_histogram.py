@@ -41,7 +41,9 @@ def check_against_oracle(oracle_lib, ux, uy, uz, bins, log_spaced, fourvel, dev,
     np.testing.assert_array_equal(c, cnt)
     if log_spaced:
         fin = np.isfinite(h64) & (h64 > 0)
-        assert np.all(np.abs(h[fin] - h64[fin]) <= 2e-7 * h64[fin])
+        # FP32 per-block partial sums flushed to FP64: ~1e-7 relative (the
+        # reference accumulates in FP32 per thread, ~1e-5)
+        assert np.all(np.abs(h[fin] - h64[fin]) <= 1e-6 * h64[fin])
         assert np.array_equal(np.isinf(h), np.isinf(h64))
     else:
         np.testing.assert_array_equal(h, cnt.astype(np.float32))
