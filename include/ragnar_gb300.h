@@ -92,6 +92,13 @@ int rg_ffunc_integrand(const float* x, int64_t n, float* y, void* stream);
  * `stream`. */
 int rg_ffunc_table(int64_t n, float xmin, float xmax, float* x, float* y, void* stream);
 
+/* The smooth (differentiable) table: exact F(x) = x int_x^inf K_{5/3} at nodes
+ * x_j = e^{ln_xmin + j dln}, j = 0..nseg, built on the GPU in FP64, as C1 cubic
+ * Hermite segments with node slopes dF/dln x = F - x^2 K_{5/3}; coef (host,
+ * nullable) receives nseg x 4 floats (c0..c3 in tau = t - j).  Extension: the
+ * reference has only the 200-point table. */
+int rg_smooth_table(float* coef, int32_t* nseg, double* ln_xmin, double* dln);
+
 /* --------------------------------------------------------------------------
  * Particle synchrotron spectrum
  * ------------------------------------------------------------------------ */
@@ -175,8 +182,42 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
                             float g_syn, float e_syn_at_g_syn, float* out, void* stream);
 
 /* --------------------------------------------------------------------------
+ * Adjoint (differentiation)
+ * ------------------------------------------------------------------------ */
+
+/* Gradient of a loss L through rg_spectrum_run: given grad_out = dL/dS (nbins
+ * device floats), writes dL/dw and dL/du (device, n floats each; any may be
+ * NULL) for every particle of `p`.  The derivative is that of the table the plan
+ * evaluates: with RG_TABLE_SMOOTH, F'(x) = F(x)/x - x K_{5/3}(x) at the table
+ * nodes and the derivative of its C1 cubic Hermite interpolant in between; with
+ * RG_TABLE_REFERENCE, the slope of the reference's log-linear segments
+ * (tabulation.hpp:39-41).  e_peak is recomputed, not stored.  Up to 512 bins.
+ * Extension: the reference has no derivative. */
+int rg_spectrum_adjoint(const rg_spectrum_plan* plan, const rg_particles* p, const float* grad_out,
+                        float* grad_w, float* grad_ux, float* grad_uy, float* grad_uz, void* stream);
+
+/* Batched adjoint: grad_out is [nseg x nbins], segments as rg_spectrum_run_batched. */
+int rg_spectrum_adjoint_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
+                                int32_t nseg, const float* grad_out, float* grad_w, float* grad_ux,
+                                float* grad_uy, float* grad_uz, void* stream);
+
+/* --------------------------------------------------------------------------
  * Spectrum from a tabulated distribution
  * ------------------------------------------------------------------------ */
+
+/* A plan for sync::KernelFromDist (synchrotron.hpp:72-95): e_peak(g) =
+ * e_syn_at_g_syn gbeta^2 / g_syn^2, amplitude f_g (times gbeta_g when the gamma
+ * bins are log-spaced).  bins is host (nbins).  Either table mode. */
+int rg_dist_plan_create(const float* bins, int32_t nbins, float g_syn, float e_syn_at_g_syn,
+                        int32_t log_spaced, int32_t table_mode, rg_spectrum_plan** plan);
+
+/* Spectrum of one distribution (gbeta, f: device, ng) into out (device, nbins). */
+int rg_dist_run(const rg_spectrum_plan* plan, const float* gbeta, const float* f, int32_t ng, float* out,
+                void* stream);
+
+/* dL/df (device, ng) given dL/dS (device, nbins). */
+int rg_dist_adjoint(const rg_spectrum_plan* plan, const float* gbeta, const float* f, int32_t ng,
+                    const float* grad_out, float* grad_f, void* stream);
 
 /* SynchrotronSpectrumFromDist (synchrotron.cpp:69-105, sync::KernelFromDist
  * synchrotron.hpp:72-95): gbeta (device, ng) and f (device, ng) describe the

@@ -87,7 +87,15 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_plan_kernel_time": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64)],
         "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
         "rg_synchrotron_spectrum_from_dist": [_vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _vp, _vp],
+        "rg_spectrum_adjoint": [_vp, ctypes.POINTER(Particles), _vp, _vp, _vp, _vp, _vp, _vp],
+        "rg_spectrum_adjoint_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp, _vp, _vp,
+                                        _vp, _vp],
+        "rg_dist_plan_create": [_vp, _i32, _f32, _f32, _i32, _i32, ctypes.POINTER(_vp)],
+        "rg_dist_run": [_vp, _vp, _vp, _i32, _vp, _vp],
+        "rg_dist_adjoint": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
+        "rg_smooth_table": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
+                            ctypes.POINTER(ctypes.c_double)],
         "rg_energy_distribution": [_vp, _vp, _vp, _i64, _vp, _i32, _i32, _i32, _vp, _vp, _vp],
     }
     for name, args in sig.items():
@@ -194,6 +202,17 @@ class SpectrumPlan:
         check(lib().rg_spectrum_plan_kernel_time(self.handle, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def adjoint(self, prt: Particles, grad_out, grad_w=None, grad_u=(None, None, None),
+                stream: int = 0) -> None:
+        check(lib().rg_spectrum_adjoint(self.handle, ctypes.byref(prt), addr(grad_out), addr(grad_w),
+                                        addr(grad_u[0]), addr(grad_u[1]), addr(grad_u[2]), stream))
+
+    def adjoint_batched(self, prt: Particles, offsets, nseg: int, grad_out, grad_w=None,
+                        grad_u=(None, None, None), stream: int = 0) -> None:
+        check(lib().rg_spectrum_adjoint_batched(self.handle, ctypes.byref(prt), addr(offsets), nseg,
+                                                addr(grad_out), addr(grad_w), addr(grad_u[0]),
+                                                addr(grad_u[1]), addr(grad_u[2]), stream))
+
     def reserve(self, nseg: int) -> None:
         check(lib().rg_spectrum_plan_reserve(self.handle, nseg))
 
@@ -210,3 +229,24 @@ class SpectrumPlan:
             self.close()
         except Exception:  # noqa: BLE001
             pass
+
+
+class DistPlan(SpectrumPlan):
+    """rg_spectrum_plan for a tabulated distribution (rg_dist_plan_create)."""
+
+    def __init__(self, bins, g_syn: float, eps: float, log_spaced: bool, mode: int = RG_TABLE_REFERENCE):
+        import numpy as np  # noqa: PLC0415
+
+        self.bins = np.ascontiguousarray(bins, dtype=np.float32)
+        self.nbins = len(self.bins)
+        h = _vp()
+        check(lib().rg_dist_plan_create(self.bins.ctypes.data, self.nbins, g_syn, eps, int(log_spaced),
+                                        mode, ctypes.byref(h)))
+        self.handle = h
+
+    def run_dist(self, gbeta, f, out, stream: int = 0) -> None:
+        check(lib().rg_dist_run(self.handle, addr(gbeta), addr(f), int(f.numel()), addr(out), stream))
+
+    def adjoint_dist(self, gbeta, f, grad_out, grad_f, stream: int = 0) -> None:
+        check(lib().rg_dist_adjoint(self.handle, addr(gbeta), addr(f), int(f.numel()), addr(grad_out),
+                                    addr(grad_f), stream))

@@ -222,7 +222,8 @@ namespace rg {
     t.dln     = std::log(kSmoothXmax / kSmoothXmin) / kSmoothSegments;
     double2* nodes = nullptr;
     RG_CUDA_TRY(cudaMalloc(&nodes, sizeof(double2) * (kSmoothSegments + 1)));
-    RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float4) * kSmoothSegments));
+    RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float4) * (kSmoothSegments + 1)));
+    RG_CUDA_TRY(cudaMemsetAsync(t.d_coef + kSmoothSegments, 0, sizeof(float4), s));
     smooth_nodes_kernel<<<(kSmoothSegments + 1 + 127) / 128, 128, 0, s>>>(kSmoothSegments + 1,
                                                                            t.ln_xmin, t.dln, nodes);
     RG_CUDA_TRY(cudaGetLastError());

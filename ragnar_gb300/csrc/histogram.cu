@@ -91,6 +91,9 @@ namespace rg {
 
     // float(1.0 / sqrt(1.0 + U)) without FP64: one Newton step in double-float.
     __device__ __forceinline__ float inv_sqrt_one_plus(float U) {
+      if (!(U < 3.0e38f)) {
+        return U == U ? 0.0f : U; // 1/sqrt(1 + inf) = 0; NaN stays NaN
+      }
       const ff    s  = two_sum(1.0f, U);
       const float r0 = rsqrtf(s.hi);
       // e = 1 - s r0^2 in double-float, r = r0 + r0 e / 2

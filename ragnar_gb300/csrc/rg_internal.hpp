@@ -47,7 +47,7 @@ namespace rg {
   constexpr double   kSlopeScale  = 1.7014118346046923e38; // 2^127
 
   // Smooth (differentiable) table: exact F on a log grid, cubic Hermite segments.
-  constexpr int    kSmoothSegments = 4096;
+  constexpr int    kSmoothSegments = 2048;
   constexpr double kSmoothXmin     = 1e-6;
   constexpr double kSmoothXmax     = 100.0;
 
@@ -62,7 +62,7 @@ namespace rg {
   };
 
   struct SmoothTable {
-    float4* d_coef  = nullptr; // kSmoothSegments (c0, c1, c2, c3) in tau
+    float4* d_coef  = nullptr; // kSmoothSegments (c0, c1, c2, c3) in tau, then one zero entry
     double  ln_xmin = 0, dln = 0;
   };
 

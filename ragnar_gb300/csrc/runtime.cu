@@ -137,6 +137,24 @@ int rg_finalize(void) {
   return RG_OK;
 }
 
+int rg_smooth_table(float* coef, int32_t* nseg, double* ln_xmin, double* dln) {
+  const rg::SmoothTable* t = nullptr;
+  RG_TRY(rg::smooth_table(&t));
+  if (nseg) {
+    *nseg = rg::kSmoothSegments;
+  }
+  if (ln_xmin) {
+    *ln_xmin = t->ln_xmin;
+  }
+  if (dln) {
+    *dln = t->dln;
+  }
+  if (coef) {
+    RG_CUDA_TRY(cudaMemcpy(coef, t->d_coef, sizeof(float4) * rg::kSmoothSegments, cudaMemcpyDeviceToHost));
+  }
+  return RG_OK;
+}
+
 int rg_device_sm_count(int* sms) {
   rg::DeviceContext* c = nullptr;
   RG_TRY(rg::context(&c));

@@ -1,4 +1,4 @@
-// Particle and distribution synchrotron spectra on sm_103a.
+// Particle and distribution synchrotron spectra on sm_103a (forward).
 //
 // Reference path: sync::Kernel<D>::operator() (synchrotron.hpp:145-172) and
 // sync::KernelFromDist::operator() (synchrotron.hpp:72-95), reduced over
@@ -9,28 +9,32 @@
 //  * Per-particle stage, once per particle: gamma^2 = 1 + u^2 and
 //    W = |gamma E + u x B|^2 - (u.E)^2 as double-floats, then
 //      chiR = sqrt(W) / (gamma B0),  e_peak = K0 gamma sqrt(W),  K0 = eps / (g^2 B0),
-//    and the particle's table coordinate Q = 2^22 (ln gamma + ln W / 2) / dln as a
-//    fixed-point integer (ln of a double-float to ~1e-10 absolute).
-//  * Photon bin b carries P_b = 2^22 (ln e_b - ln xmin - ln K0) / dln (host, FP64),
-//    so T = P_b - Q (one 32-bit integer add, exact) is the fixed-point table
-//    coordinate of x = e_b / e_peak.  Its top 10 bits index a 1024-entry segment
-//    table in shared memory (entries past the last segment are zero, so an
-//    out-of-range x reads zero without a branch); its low 22 bits, read as a
-//    denormal, times the stored slope (pre-scaled by 2^127) give frac * slope in
-//    one FFMA.  Per eval: IADD, SHF, LOP, LDS.64, FFMA (F), FFMA (accumulate).
+//    and the particle's table coordinate Q = 2^frac (ln gamma + ln W / 2) / dln
+//    as a fixed-point integer (ln of a double-float to ~1e-10 absolute).
+//  * Photon bin b carries P_b = 2^frac (ln e_b - ln xmin - ln K0) / dln (host,
+//    FP64), so T = P_b - Q (one 32-bit integer add, exact) is the fixed-point
+//    table coordinate of x = e_b / e_peak.
+//      reference table (frac = 22): the top 10 bits of T index a 1024-entry
+//      segment table in shared memory whose entries past the last segment are
+//      zero, so an out-of-range x reads zero without a branch; the low 22 bits,
+//      read as a denormal, times the stored slope (pre-scaled by 2^127) give
+//      frac * slope in one FFMA.  Per eval: IADD, SHF, LOP, LDS.64, FFMA (F),
+//      FFMA (accumulate).
+//      smooth table: T >> frac (clamped to a zero entry) indexes cubic Hermite
+//      segments; tau = (T & mask) 2^-frac; three FFMAs evaluate the cubic.
 //  * Lanes own photon bins (32 consecutive bins per row, K rows per lane), warps
 //    own particles; per-warp FP32 register accumulators are folded into
-//    double-float accumulators after every chunk, combined across warps in FP64
-//    in a fixed order and written per block; a second kernel sums the blocks in
-//    FP64 in a fixed order, so results are bit-reproducible.
+//    double-float accumulators after every chunk and flushed per warp to FP64
+//    scratch; a second kernel sums blocks and warps in FP64 in a fixed order, so
+//    results are bit-reproducible.
 //  * Particle streams (SoA FP32) are staged chunk by chunk into shared memory
 //    with 1-D TMA bulk copies (cp.async.bulk + mbarrier), double buffered.
 //  * Work items are (segment, chunk) pairs in particle order; each block of the
 //    persistent grid takes a contiguous range of items, so one spectrum and a
 //    batch of uneven segments run through the same launch, and every block
 //    touches each segment in one contiguous run (one partial per (block, seg)).
-#include "rg_common.cuh"
-#include "rg_internal.hpp"
+#include "spectrum_common.cuh"
+#include "spectrum_plan.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -46,245 +50,26 @@ namespace rg {
 
   namespace {
 
-    constexpr int kThreads   = 256;
-    constexpr int kWarps     = kThreads / 32;
-    constexpr int kSliceBins = 512; // bins per block slice (K <= 16 rows of 32)
-    constexpr int kChunk     = 512; // particles per work item
-    constexpr int kChunkPad  = kChunk + 4;
-    constexpr int kComps     = 10;  // u0 u1 u2 e0 e1 e2 b0 b1 b2 w
-    constexpr int kBlocksPerSM = 2;
-
-    // extra status bit: segment offsets were not non-decreasing
-    constexpr unsigned kDevBadOffsets = 4u;
-
-    enum Source : int { kSrcParticles = 0, kSrcDist = 1 };
-
-    struct FusedParams {
-      const float*   comp[kComps]; // particle streams (dist: comp[0] = gbeta, comp[1] = f)
-      int            slot[kComps]; // shared-memory stream slot, -1 if not staged
-      int            nslots;
-      int            source;
-      int            has_e;
-      int            has_w;
-      int            use_tma;
-      int            log_spaced;   // dist: J_g = gbeta when set
-      const int64_t* seg_off;      // nseg + 1 particle offsets (device), or null: one segment
-      const int64_t* item_prefix;  // nseg + 1 cumulative item counts (device), or null
-      int64_t        n_single;     // particle count when seg_off is null
-      int            nseg;
-      const int32_t* P;            // nslices * kSliceBins fixed-point bin coordinates
-      const int64_t* Prange;       // per slice: (Pmin, Pmax) over valid bins
-      int64_t        L;            // (n_nodes - 1) << kFrac
-      float          Sh, Sl;       // 2^kFrac / (2 dln) as a double-float
-      int64_t        Cfx;          // round(S ln2 2^16)
-      float          amp;          // 1 / B0 (particles) or 1 (dist)
-      const float2*  table;        // kRefEntries segments
-      double*        partials;     // [(grid + nseg) * nslices * kSliceBins]
-      int            nslices;
-      unsigned*      status;
-    };
-
-    struct ItemInfo {
-      int     seg;
-      int     np;
-      int64_t pstart, pend, a0, a1;
-    };
-
-    __device__ __forceinline__ int64_t seg_begin(const FusedParams& p, int s) {
-      return p.seg_off ? p.seg_off[s] : 0;
-    }
-
-    __device__ __forceinline__ int64_t seg_end(const FusedParams& p, int s) {
-      return p.seg_off ? p.seg_off[s + 1] : p.n_single;
-    }
-
-    __device__ __forceinline__ int64_t items_before(const int64_t* prefix, int s) {
-      return prefix ? prefix[s] : 0;
-    }
-
-    __device__ __forceinline__ int64_t total_items(const int64_t* prefix, int nseg,
-                                                   int64_t n_single) {
-      return prefix ? prefix[nseg] : (n_single + kChunk - 1) / kChunk;
-    }
-
-    // ---- accurate logarithm of a positive double-float ---------------------------
-    struct LnParts {
-      int   e; // ln x = e ln2 + h + l
-      float h, l;
-    };
-
-    __device__ __forceinline__ LnParts ln_parts(ff x) {
-      int   e;
-      float m = frexpf(x.hi, &e); // x.hi = m 2^e, m in [0.5, 1)
-      if (m < 0.70710678f) {
-        m = __fmul_rn(m, 2.0f);
-        e -= 1;
-      }
-      // ln m = 2 atanh(z), z = (m - 1)/(m + 1), |z| < 0.1716
-      const float f  = __fsub_rn(m, 1.0f); // exact
-      const ff    d  = two_sum(m, 1.0f);
-      const float q  = __fdiv_rn(f, d.hi);
-      const float r  = __fmaf_rn(-q, d.hi, f); // exact remainder
-      const float zl = __fdiv_rn(__fmaf_rn(-q, d.lo, r), d.hi);
-      const float w  = __fmul_rn(q, q);
-      const float poly =
-        w * (0.33333334f + w * (0.2f + w * (0.14285715f + w * (0.11111111f + w * 0.09090909f))));
-      LnParts o;
-      o.e = e;
-      o.h = __fmul_rn(2.0f, q);
-      o.l = __fadd_rn(__fmaf_rn(o.h, poly, __fmul_rn(2.0f, zl)), __fdiv_rn(x.lo, x.hi));
-      return o;
-    }
-
-    // round(S (ln X1 + ln X2)), S = Sh + Sl; the exponent part goes through the
-    // integer constant Cfx = round(S ln2 2^16).
-    __device__ __forceinline__ int64_t fixed_log_sum(ff X1, ff X2, float Sh, float Sl,
-                                                     int64_t Cfx) {
-      const LnParts a = ln_parts(X1);
-      const LnParts b = ln_parts(X2);
-      ff            s = two_sum(a.h, b.h);
-      s.lo            = __fadd_rn(s.lo, __fadd_rn(a.l, b.l));
-      const float ph  = __fmul_rn(s.hi, Sh);
-      const float pe  = __fmaf_rn(s.hi, Sh, -ph);
-      const float pl  = __fadd_rn(pe, __fmaf_rn(s.hi, Sl, __fmul_rn(s.lo, Sh)));
-      const int64_t q = static_cast<int64_t>(a.e + b.e) * Cfx +
-                        __float2ll_rn(__fmul_rn(ph, 65536.0f)) +
-                        __float2ll_rn(__fmul_rn(pl, 65536.0f));
-      return (q + 32768) >> 16;
-    }
-
-    // Per-particle stage for particle data.  Returns false if the particle adds
-    // nothing (e_peak <= 0 or not finite, or x outside the table for every bin).
-    __device__ __forceinline__ bool particle_stage(const float (&v)[kComps], const FusedParams& p,
-                                                   int64_t Pmin, int64_t Pmax, uint32_t& q32,
-                                                   float& A) {
-      const float ux = v[0], uy = v[1], uz = v[2];
-      const float bx = v[6], by = v[7], bz = v[8];
-      ff          u2 = two_prod(ux, ux);
-      u2             = ff_add(u2, two_prod(uy, uy));
-      u2             = ff_add(u2, two_prod(uz, uz));
-      const ff G     = ff_add(ff { 1.0f, 0.0f }, u2);
-      const ff cx    = ff_diff_of_products(uy, bz, uz, by);
-      const ff cy    = ff_diff_of_products(uz, bx, ux, bz);
-      const ff cz    = ff_diff_of_products(ux, by, uy, bx);
-      ff       W;
-      if (!p.has_e) {
-        W = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
-      } else {
-        const float ex = v[3], ey = v[4], ez = v[5];
-        // gamma as a double-float: g = sqrt(G.hi), correction (G - g^2) / (2 g)
-        const float gh = sqrtf(G.hi);
-        const float gl = __fdiv_rn(__fadd_rn(__fmaf_rn(-gh, gh, G.hi), G.lo), __fmul_rn(2.0f, gh));
-        const ff    gm { gh, gl };
-        const ff    Vx = ff_add(ff_mul(gm, ff { ex, 0.0f }), cx);
-        const ff    Vy = ff_add(ff_mul(gm, ff { ey, 0.0f }), cy);
-        const ff    Vz = ff_add(ff_mul(gm, ff { ez, 0.0f }), cz);
-        ff          uE = two_prod(ux, ex);
-        uE             = ff_add(uE, two_prod(uy, ey));
-        uE             = ff_add(uE, two_prod(uz, ez));
-        W = ff_add(ff_add(ff_add(ff_sqr(Vx), ff_sqr(Vy)), ff_sqr(Vz)), ff_neg(ff_sqr(uE)));
-      }
-      if (!(W.hi > 0.0f) || !isfinite(W.hi) || !isfinite(G.hi)) {
-        return false;
-      }
-      const int64_t Q = fixed_log_sum(G, W, p.Sh, p.Sl, p.Cfx);
-      if (Q <= Pmin - p.L || Q > Pmax) {
-        return false;
-      }
-      q32 = static_cast<uint32_t>(Q);
-      A   = p.amp * sqrtf(__fdiv_rn(W.hi, G.hi));
-      if (p.has_w) {
-        A *= v[9];
-      }
-      return isfinite(A);
-    }
-
-    // Per-"particle" stage of a tabulated distribution (synchrotron.hpp:76-94):
-    // e_peak = K0 gbeta^2, amplitude f * (gbeta if the gamma bins are log-spaced).
-    __device__ __forceinline__ bool dist_stage(float gb, float f, const FusedParams& p,
-                                               int64_t Pmin, int64_t Pmax, uint32_t& q32,
-                                               float& A) {
-      const ff X = two_prod(gb, gb);
-      if (!(X.hi > 0.0f) || !isfinite(X.hi)) {
-        return false;
-      }
-      const int64_t Q = fixed_log_sum(X, X, p.Sh, p.Sl, p.Cfx);
-      if (Q <= Pmin - p.L || Q > Pmax) {
-        return false;
-      }
-      q32 = static_cast<uint32_t>(Q);
-      A   = p.log_spaced ? __fmul_rn(f, gb) : f;
-      return isfinite(A);
-    }
-
-    __device__ __forceinline__ ItemInfo item_info(const FusedParams& p, int64_t i, int& seg_hint) {
-      int s = seg_hint;
-      while (s + 1 < p.nseg && items_before(p.item_prefix, s + 1) <= i) {
-        ++s;
-      }
-      seg_hint        = s;
-      const int64_t c = i - items_before(p.item_prefix, s);
-      ItemInfo      I;
-      I.seg    = s;
-      I.pstart = seg_begin(p, s) + c * kChunk;
-      I.pend   = min(I.pstart + kChunk, seg_end(p, s));
-      I.np     = static_cast<int>(I.pend - I.pstart);
-      I.a0     = I.pstart & ~int64_t(3);
-      I.a1     = I.pend & ~int64_t(3);
-      if (I.a1 < I.a0) {
-        I.a1 = I.a0;
-      }
-      return I;
-    }
-
-    __device__ __forceinline__ void issue_stage(const FusedParams& p, const ItemInfo& I,
-                                                float* buf, uint64_t* bar) {
-      const uint32_t bytes = static_cast<uint32_t>(I.a1 - I.a0) * 4u;
-      mbar_arrive_expect_tx(bar, bytes * static_cast<uint32_t>(p.nslots));
-      if (bytes) {
-        for (int c = 0; c < kComps; ++c) {
-          if (p.slot[c] >= 0) {
-            bulk_g2s(buf + p.slot[c] * kChunkPad, p.comp[c] + I.a0, bytes, bar);
-          }
-        }
-      }
-    }
-
-    // Block b of G owns items [b n / G, (b+1) n / G); the block holding item i:
-    __device__ __forceinline__ int block_of_item(int64_t i, int64_t n_items, int G) {
-      return static_cast<int>(((i + 1) * G - 1) / n_items);
-    }
-
     template <int K>
-    __device__ __forceinline__ void flush_block(float (&hi)[K], float (&lo)[K], double* red,
-                                                double* dst, int warp, int lane, int tid) {
+    __device__ __forceinline__ void flush_warp(float (&hi)[K], float (&lo)[K], double* dst, int lane) {
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        red[warp * kSliceBins + k * 32 + lane] =
-          static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
-        hi[k] = 0.0f;
-        lo[k] = 0.0f;
+        dst[k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
+        hi[k]              = 0.0f;
+        lo[k]              = 0.0f;
       }
-      __syncthreads();
-      for (int j = tid; j < K * 32; j += kThreads) {
-        double s = 0.0;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-          s += red[w * kSliceBins + j];
-        }
-        dst[j] = s;
-      }
-      __syncthreads();
     }
 
-    template <int K>
+    template <int K, int MODE>
     __global__ void __launch_bounds__(kThreads, kBlocksPerSM)
       fused_spectrum_kernel(const __grid_constant__ FusedParams p) {
       extern __shared__ __align__(128) unsigned char smem[];
-      float2* tab   = reinterpret_cast<float2*>(smem);
-      int2*   qa    = reinterpret_cast<int2*>(smem + sizeof(float2) * kRefEntries);
-      double* red   = reinterpret_cast<double*>(qa + 2 * kChunk);
-      float*  stage = reinterpret_cast<float*>(red + kWarps * kSliceBins);
+      float2* tab  = reinterpret_cast<float2*>(smem);
+      float4* htab = reinterpret_cast<float4*>(smem);
+      const int tab_size = (MODE == kModeRef) ? static_cast<int>(sizeof(float2)) * kRefEntries
+                                              : static_cast<int>(sizeof(float4)) * (p.hseg + 1);
+      int2*  qa    = reinterpret_cast<int2*>(smem + tab_size);
+      float* stage = reinterpret_cast<float*>(qa + 2 * kChunk);
       __shared__ uint64_t mbar[2];
       __shared__ ItemInfo info[2];
 
@@ -297,16 +82,27 @@ namespace rg {
       if (it_begin >= it_end || *p.status != kDevOk) {
         return;
       }
-      for (int i = tid; i < kRefEntries; i += kThreads) {
-        tab[i] = p.table[i];
+      if (MODE == kModeRef) {
+        for (int i = tid; i < kRefEntries; i += kThreads) {
+          tab[i] = p.table[i];
+        }
+      } else {
+        for (int i = tid; i <= p.hseg; i += kThreads) {
+          htab[i] = p.htable[i];
+        }
       }
       int32_t P[K];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         P[k] = p.P[slice * kSliceBins + k * 32 + lane];
       }
-      const int64_t Pmin = p.Prange[2 * slice], Pmax = p.Prange[2 * slice + 1];
-      const int     stage_floats = p.nslots * kChunkPad;
+      const int64_t  Pmin = p.Prange[2 * slice], Pmax = p.Prange[2 * slice + 1];
+      const int      stage_floats = p.nslots * kChunkPad;
+      const uint32_t dead         = dead_coordinate(Pmin, p.L);
+      const int      frac         = (MODE == kModeRef) ? kFrac : p.frac;
+      const uint32_t fmask        = (1u << frac) - 1u;
+      const uint32_t hseg         = static_cast<uint32_t>(p.hseg);
+      const float    tau_scale    = p.tau_scale;
 
       int seg_hint = 0;
       if (tid == 0) {
@@ -354,10 +150,7 @@ namespace rg {
         const ItemInfo I = info[st];
         if (I.seg != cur_seg) {
           if (cur_seg >= 0) {
-            flush_block<K>(hi, lo, red,
-                           p.partials + (static_cast<int64_t>(b + cur_seg) * p.nslices + slice) *
-                                          kSliceBins,
-                           warp, lane, tid);
+            flush_warp<K>(hi, lo, warp_partial(p, b, cur_seg, slice, warp), lane);
           }
           cur_seg = I.seg;
         }
@@ -366,23 +159,14 @@ namespace rg {
         const float* sbuf = stage + st * stage_floats;
         int2*        qdst = qa + st * kChunk;
         for (int j = tid; j < I.np; j += kThreads) {
-          const int64_t gp      = I.pstart + j;
-          const bool    in_smem = p.use_tma && gp < I.a1;
-          float         v[kComps];
-#pragma unroll
-          for (int c = 0; c < kComps; ++c) {
-            const float* src = p.comp[c];
-            v[c]             = 0.0f;
-            if (src) {
-              v[c] = in_smem ? sbuf[p.slot[c] * kChunkPad + (gp - I.a0)] : __ldg(src + gp);
-            }
-          }
-          uint32_t q = 0;
-          float    A = 0.0f;
+          float v[kComps];
+          load_comps(p, I, sbuf, I.pstart + j, v);
+          uint32_t   q    = 0;
+          float      A    = 0.0f;
           const bool live = (p.source == kSrcParticles) ? particle_stage(v, p, Pmin, Pmax, q, A)
                                                         : dist_stage(v[0], v[1], p, Pmin, Pmax, q, A);
           if (!live) {
-            q = 0;
+            q = dead;
             A = 0.0f;
           }
           qdst[j] = make_int2(static_cast<int>(q), __float_as_int(A));
@@ -400,10 +184,17 @@ namespace rg {
 #pragma unroll
           for (int k = 0; k < K; ++k) {
             const uint32_t T = static_cast<uint32_t>(P[k]) - q;
-            const float2   c = tab[T >> kFrac];
-            const float    m = __uint_as_float(T & kFracMask);
-            const float    F = __fmaf_rn(m, c.y, c.x);
-            acc[k]           = __fmaf_rn(A, F, acc[k]);
+            if (MODE == kModeRef) {
+              const float2 c = tab[T >> kFrac];
+              const float  m = __uint_as_float(T & kFracMask);
+              const float  F = __fmaf_rn(m, c.y, c.x);
+              acc[k]         = __fmaf_rn(A, F, acc[k]);
+            } else {
+              const float4 c   = htab[min(T >> frac, hseg)];
+              const float  tau = __uint2float_rn(T & fmask) * tau_scale;
+              const float  F   = __fmaf_rn(tau, __fmaf_rn(tau, __fmaf_rn(tau, c.w, c.z), c.y), c.x);
+              acc[k]           = __fmaf_rn(A, F, acc[k]);
+            }
           }
         }
 #pragma unroll
@@ -415,16 +206,13 @@ namespace rg {
         }
       }
       if (cur_seg >= 0) {
-        flush_block<K>(hi, lo, red,
-                       p.partials + (static_cast<int64_t>(b + cur_seg) * p.nslices + slice) *
-                                      kSliceBins,
-                       warp, lane, tid);
+        flush_warp<K>(hi, lo, warp_partial(p, b, cur_seg, slice, warp), lane);
       }
     }
 
     // Cumulative chunk counts of the segments (one block), with a check that the
     // offsets never decrease and stay within [0, n]; on failure the status word
-    // is set and the fused kernel that follows does no work.
+    // is set and the kernels that follow do no work.
     __global__ void item_prefix_kernel(const int64_t* __restrict__ off, int nseg, int64_t n,
                                        int64_t* __restrict__ prefix, unsigned* status) {
       __shared__ int64_t carry;
@@ -446,7 +234,6 @@ namespace rg {
             v = (e - a + kChunk - 1) / kChunk;
           }
         }
-        // inclusive scan within the warp, then across warps
         for (int o = 1; o < 32; o <<= 1) {
           const int64_t t = __shfl_up_sync(0xffffffffu, v, o);
           if (lane >= o) {
@@ -480,7 +267,7 @@ namespace rg {
       }
     }
 
-    // Sums the per-block partials of every (segment, bin) in block order and
+    // Sums the per-warp partials of every (segment, bin) in (block, warp) order and
     // applies the photon-energy factor; masked bins are zero, and every output is
     // NaN if the device status reports a failure.
     struct ReduceParams {
@@ -517,7 +304,12 @@ namespace rg {
           const int slice = bin / kSliceBins, j = bin % kSliceBins;
           double    sum   = 0.0;
           for (int b = b0; b <= b1; ++b) {
-            sum += r.partials[(static_cast<int64_t>(b + s) * r.nslices + slice) * kSliceBins + j];
+            const double* base =
+              r.partials + (static_cast<int64_t>(b + s) * r.nslices + slice) * kWarps * kSliceBins + j;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+              sum += base[w * kSliceBins];
+            }
           }
           result = sum * static_cast<double>(r.ebins[bin]);
         }
@@ -530,8 +322,8 @@ namespace rg {
       }
     }
 
-    __global__ void finalize_acc_kernel(const double* __restrict__ acc, int n,
-                                        const unsigned* status, float* __restrict__ out) {
+    __global__ void finalize_acc_kernel(const double* __restrict__ acc, int n, const unsigned* status,
+                                        float* __restrict__ out) {
       const int i = blockIdx.x * blockDim.x + threadIdx.x;
       if (i < n) {
         out[i] = (*status != kDevOk) ? __int_as_float(0x7fc00000) : __double2float_rn(acc[i]);
@@ -636,32 +428,33 @@ namespace rg {
       }
     }
 
-    size_t fused_smem(int nslots) {
-      return sizeof(float2) * kRefEntries + sizeof(int2) * 2 * kChunk +
-             sizeof(double) * kWarps * kSliceBins + sizeof(float) * 2 * nslots * kChunkPad;
+    size_t fused_smem(int mode, int hseg, int nslots) {
+      const size_t tab = (mode == kModeRef) ? sizeof(float2) * kRefEntries : sizeof(float4) * (hseg + 1);
+      return tab + sizeof(int2) * 2 * kChunk + sizeof(float) * 2 * nslots * kChunkPad;
     }
 
-    template <int K>
+    template <int K, int MODE>
     cudaError_t launch_fused_k(const FusedParams& fp, dim3 grid, size_t smem, cudaStream_t s) {
       static bool configured = false;
       if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(fused_spectrum_kernel<K>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(fused_smem(kComps)));
+        const cudaError_t e =
+          cudaFuncSetAttribute(fused_spectrum_kernel<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)));
         if (e != cudaSuccess) {
           return e;
         }
         configured = true;
       }
-      fused_spectrum_kernel<K><<<grid, kThreads, smem, s>>>(fp);
+      fused_spectrum_kernel<K, MODE><<<grid, kThreads, smem, s>>>(fp);
       return cudaGetLastError();
     }
 
-    cudaError_t launch_fused(int K, const FusedParams& fp, dim3 grid, size_t smem, cudaStream_t s) {
+    template <int MODE>
+    cudaError_t launch_fused_mode(int K, const FusedParams& fp, dim3 grid, size_t smem, cudaStream_t s) {
       switch (K) {
 #define RG_K_CASE(k)                                                                         \
   case k:                                                                                    \
-    return launch_fused_k<k>(fp, grid, smem, s);
+    return launch_fused_k<k, MODE>(fp, grid, smem, s);
         RG_K_CASE(1) RG_K_CASE(2) RG_K_CASE(3) RG_K_CASE(4) RG_K_CASE(5) RG_K_CASE(6)
         RG_K_CASE(7) RG_K_CASE(8) RG_K_CASE(9) RG_K_CASE(10) RG_K_CASE(11) RG_K_CASE(12)
         RG_K_CASE(13) RG_K_CASE(14) RG_K_CASE(15) RG_K_CASE(16)
@@ -671,81 +464,63 @@ namespace rg {
       }
     }
 
-  } // namespace
-
-} // namespace rg
-
-// ---------------------------------------------------------------------------------
-// Plans
-// ---------------------------------------------------------------------------------
-
-struct rg_spectrum_plan {
-  int                 device     = 0;
-  int                 table_mode = RG_TABLE_REFERENCE;
-  int                 source     = rg::kSrcParticles;
-  int                 nbins      = 0;
-  int                 nslices    = 0;
-  int                 K          = 0;
-  bool                zero       = false; // every contribution is zero (K0 <= 0 ...)
-  float               B0 = 1, g_syn = 1, eps = 1;
-  int                 log_spaced = 0; // dist source
-  int64_t             L          = 0;
-  float               Sh = 0, Sl = 0;
-  int64_t             Cfx        = 0;
-  float               amp        = 1;
-  int                 grid       = 0; // blocks per slice of the fused kernel
-  std::vector<float>  h_bins;
-  int32_t*            d_P         = nullptr;
-  int64_t*            d_Prange    = nullptr;
-  float*              d_ebins     = nullptr;
-  uint8_t*            d_valid     = nullptr;
-  unsigned*           d_status    = nullptr;
-  double*             d_partials  = nullptr;
-  size_t              partial_cap = 0; // doubles
-  int64_t*            d_prefix    = nullptr;
-  int                 prefix_cap  = 0; // segments
-  double*             d_plain_acc = nullptr;
-  const rg::RefTable* ref         = nullptr;
-  // kernel timing (events bracketing each fused launch)
-  bool                                             timing = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
-  // host-resident streaming: device staging for two chunks, a copy stream
-  float*       d_stage[2]     = { nullptr, nullptr };
-  int64_t      stage_chunk    = 0;
-  cudaStream_t copy_stream    = nullptr;
-  cudaEvent_t  copied[2]      = { nullptr, nullptr };
-  cudaEvent_t  consumed[2]    = { nullptr, nullptr };
-  double*      d_acc64        = nullptr;
-};
-
-namespace rg {
-
-  namespace {
-
-    int plan_reserve(rg_spectrum_plan* pl, int max_seg) {
-      const size_t need = static_cast<size_t>(pl->grid + max_seg) * pl->nslices * kSliceBins;
-      if (need > pl->partial_cap) {
-        cudaFree(pl->d_partials);
-        pl->d_partials = nullptr;
-        RG_CUDA_TRY(cudaMalloc(&pl->d_partials, sizeof(double) * need));
-        pl->partial_cap = need;
+    int timed_launch(rg_spectrum_plan* pl, const FusedParams& fp, dim3 grid, size_t smem,
+                     cudaStream_t s) {
+      std::pair<cudaEvent_t, cudaEvent_t> ev { nullptr, nullptr };
+      if (pl->timing) {
+        if (pl->ev_free.empty()) {
+          RG_CUDA_TRY(cudaEventCreate(&ev.first));
+          RG_CUDA_TRY(cudaEventCreate(&ev.second));
+        } else {
+          ev = pl->ev_free.back();
+          pl->ev_free.pop_back();
+        }
+        RG_CUDA_TRY(cudaEventRecord(ev.first, s));
       }
-      if (max_seg > pl->prefix_cap) {
-        cudaFree(pl->d_prefix);
-        pl->d_prefix = nullptr;
-        RG_CUDA_TRY(cudaMalloc(&pl->d_prefix, sizeof(int64_t) * (max_seg + 1)));
-        pl->prefix_cap = max_seg;
+      const cudaError_t e = (pl->table_mode == kModeRef)
+                              ? launch_fused_mode<kModeRef>(pl->K, fp, grid, smem, s)
+                              : launch_fused_mode<kModeSmooth>(pl->K, fp, grid, smem, s);
+      RG_CUDA_TRY(e);
+      if (pl->timing) {
+        RG_CUDA_TRY(cudaEventRecord(ev.second, s));
+        pl->ev_used.push_back(ev);
       }
       return RG_OK;
     }
 
-    // Fixed-point coordinates of the photon bins (FP64 on the host).  Fails if one
-    // 512-bin slice spans more than the 32-bit window allows (about 33 decades).
-    int plan_prepare_bins(rg_spectrum_plan* pl, double ln_xmin, double dln, int n_nodes,
+    // Fixed-point coordinates of the photon bins (FP64 on the host).  For the
+    // smooth table the fraction bits are chosen so that every slice's bin span
+    // plus the table fits the 32-bit window; the reference table uses kFrac and
+    // fails if a 512-bin slice spans more than about 33 decades.
+    int plan_prepare_bins(rg_spectrum_plan* pl, double ln_xmin, double dln, int nseg_table,
                           double ln_k0) {
-      const double scale = std::ldexp(1.0, kFrac) / dln;
-      pl->L              = static_cast<int64_t>(n_nodes - 1) << kFrac;
-      const double S     = std::ldexp(1.0, kFrac) / (2.0 * dln);
+      // span of the valid bins of each slice, in table segments
+      double max_span = 0.0;
+      for (int s = 0; s < pl->nslices; ++s) {
+        double lo = std::numeric_limits<double>::max(), hi = -lo;
+        for (int j = 0; j < kSliceBins && s * kSliceBins + j < pl->nbins; ++j) {
+          const double e = pl->h_bins[s * kSliceBins + j];
+          if (e > 0.0 && std::isfinite(e)) {
+            lo = std::min(lo, std::log(e));
+            hi = std::max(hi, std::log(e));
+          }
+        }
+        if (hi >= lo) {
+          max_span = std::max(max_span, (hi - lo) / dln);
+        }
+      }
+      if (pl->table_mode == kModeRef) {
+        pl->frac = kFrac;
+      } else {
+        const double room = 4294967296.0 / (max_span + nseg_table + 2.0);
+        pl->frac          = std::min(kFrac, static_cast<int>(std::floor(std::log2(room))));
+        if (pl->frac < 12) {
+          return set_error(RG_ERR_UNSUPPORTED, "photon bins span too many decades for the smooth table");
+        }
+      }
+      const double scale = std::ldexp(1.0, pl->frac) / dln;
+      pl->L              = static_cast<int64_t>(nseg_table) << pl->frac;
+      const double S     = std::ldexp(1.0, pl->frac) / (2.0 * dln);
       pl->Sh             = static_cast<float>(S);
       pl->Sl             = static_cast<float>(S - static_cast<double>(pl->Sh));
       pl->Cfx            = std::llround(S * M_LN2 * 65536.0);
@@ -785,16 +560,15 @@ namespace rg {
                            "window (about 33 decades)");
         }
         for (int j = 0; j < kSliceBins; ++j) {
-          const int     bidx = s * kSliceBins + j;
-          const int64_t v    = (bidx < pl->nbins && hV[bidx]) ? Ps[j] : pmin;
+          const int     bidx     = s * kSliceBins + j;
+          const int64_t v        = (bidx < pl->nbins && hV[bidx]) ? Ps[j] : pmin;
           hP[s * kSliceBins + j] = static_cast<int32_t>(static_cast<uint32_t>(v & 0xffffffffLL));
         }
         hR[2 * s]     = pmin;
         hR[2 * s + 1] = pmax;
       }
       RG_CUDA_TRY(cudaMemcpy(pl->d_P, hP.data(), sizeof(int32_t) * nsb, cudaMemcpyHostToDevice));
-      RG_CUDA_TRY(cudaMemcpy(pl->d_Prange, hR.data(), sizeof(int64_t) * hR.size(),
-                             cudaMemcpyHostToDevice));
+      RG_CUDA_TRY(cudaMemcpy(pl->d_Prange, hR.data(), sizeof(int64_t) * hR.size(), cudaMemcpyHostToDevice));
       RG_CUDA_TRY(cudaMemcpy(pl->d_valid, hV.data(), hV.size(), cudaMemcpyHostToDevice));
       if (pl->nbins) {
         RG_CUDA_TRY(cudaMemcpy(pl->d_ebins, pl->h_bins.data(), sizeof(float) * pl->nbins,
@@ -814,7 +588,7 @@ namespace rg {
       pl->K       = nbins > kSliceBins ? 16 : std::max(1, (nbins + 31) / 32);
       DeviceContext* ctx = nullptr;
       RG_TRY(context(&ctx));
-      pl->grid = ctx->sms * kBlocksPerSM;
+      pl->grid         = ctx->sms * kBlocksPerSM;
       const size_t nsb = static_cast<size_t>(pl->nslices) * kSliceBins;
       RG_CUDA_TRY(cudaMalloc(&pl->d_P, sizeof(int32_t) * nsb));
       RG_CUDA_TRY(cudaMalloc(&pl->d_Prange, sizeof(int64_t) * 2 * pl->nslices));
@@ -823,36 +597,114 @@ namespace rg {
       RG_CUDA_TRY(cudaMalloc(&pl->d_status, sizeof(unsigned)));
       RG_CUDA_TRY(cudaMemset(pl->d_status, 0, sizeof(unsigned)));
       RG_TRY(reference_table(&pl->ref));
+      if (pl->table_mode == kModeSmooth) {
+        RG_TRY(smooth_table(&pl->smooth));
+      }
       return RG_OK;
     }
 
-    int timed_launch(rg_spectrum_plan* pl, const FusedParams& fp, dim3 grid, size_t smem,
-                     cudaStream_t s) {
-      std::pair<cudaEvent_t, cudaEvent_t> ev { nullptr, nullptr };
-      if (pl->timing) {
-        if (pl->ev_free.empty()) {
-          RG_CUDA_TRY(cudaEventCreate(&ev.first));
-          RG_CUDA_TRY(cudaEventCreate(&ev.second));
-        } else {
-          ev = pl->ev_free.back();
-          pl->ev_free.pop_back();
-        }
-        RG_CUDA_TRY(cudaEventRecord(ev.first, s));
+    // Table geometry of the plan: (ln xmin, dln, segments).
+    void table_geometry(const rg_spectrum_plan* pl, double& ln_xmin, double& dln, int& nseg) {
+      if (pl->table_mode == kModeRef) {
+        ln_xmin = pl->ref->ln_xmin;
+        dln     = pl->ref->dln;
+        nseg    = pl->ref->n - 1;
+      } else {
+        ln_xmin = pl->smooth->ln_xmin;
+        dln     = pl->smooth->dln;
+        nseg    = kSmoothSegments;
       }
-      RG_CUDA_TRY(launch_fused(pl->K, fp, grid, smem, s));
-      if (pl->timing) {
-        RG_CUDA_TRY(cudaEventRecord(ev.second, s));
-        pl->ev_used.push_back(ev);
-      }
-      return RG_OK;
     }
+
+  } // namespace
+
+  int plan_reserve(rg_spectrum_plan* pl, int max_seg) {
+    const size_t need = static_cast<size_t>(pl->grid + max_seg) * pl->nslices * kWarps * kSliceBins;
+    if (need > pl->partial_cap) {
+      cudaFree(pl->d_partials);
+      pl->d_partials = nullptr;
+      RG_CUDA_TRY(cudaMalloc(&pl->d_partials, sizeof(double) * need));
+      pl->partial_cap = need;
+    }
+    if (max_seg > pl->prefix_cap) {
+      cudaFree(pl->d_prefix);
+      pl->d_prefix = nullptr;
+      RG_CUDA_TRY(cudaMalloc(&pl->d_prefix, sizeof(int64_t) * (max_seg + 1)));
+      pl->prefix_cap = max_seg;
+    }
+    return RG_OK;
+  }
+
+  void particle_comps(const rg_particles* p, const float* out[kComps]) {
+    for (int d = 0; d < 3; ++d) {
+      out[d]     = p->u[d];
+      out[3 + d] = p->e[d];
+      out[6 + d] = p->b[d];
+    }
+    out[9] = p->w;
+  }
+
+  int check_particles(const rg_particles* p) {
+    if (!p || p->n < 0 || (p->n > 0 && (!p->u[0] || !p->u[1] || !p->u[2]))) {
+      return set_error(RG_ERR_ARGUMENT, "particles need U1..U3 device arrays and n >= 0");
+    }
+    return RG_OK;
+  }
+
+  int fill_params(const rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off,
+                  const int64_t* d_prefix, int64_t n_single, int nseg, FusedParams& fp) {
+    fp          = FusedParams {};
+    int  nslots = 0;
+    bool aligned = true;
+    for (int c = 0; c < kComps; ++c) {
+      fp.comp[c] = comp[c];
+      fp.slot[c] = -1;
+      if (comp[c]) {
+        fp.slot[c] = nslots++;
+        aligned    = aligned && (reinterpret_cast<uintptr_t>(comp[c]) % 16 == 0);
+      }
+    }
+    fp.nslots      = nslots;
+    fp.use_tma     = aligned ? 1 : 0;
+    fp.source      = pl->source;
+    fp.has_e       = (comp[3] || comp[4] || comp[5]) ? 1 : 0;
+    fp.has_w       = comp[9] ? 1 : 0;
+    fp.log_spaced  = pl->log_spaced;
+    fp.seg_off     = d_off;
+    fp.item_prefix = d_prefix;
+    fp.n_single    = n_single;
+    fp.nseg        = nseg;
+    fp.P           = pl->d_P;
+    fp.Prange      = pl->d_Prange;
+    fp.L           = pl->L;
+    fp.Sh          = pl->Sh;
+    fp.Sl          = pl->Sl;
+    fp.Cfx         = pl->Cfx;
+    fp.amp         = pl->amp;
+    fp.table       = pl->ref->d_coef;
+    fp.htable      = pl->smooth ? pl->smooth->d_coef : nullptr;
+    fp.hseg        = kSmoothSegments;
+    fp.frac        = pl->frac;
+    fp.tau_scale   = static_cast<float>(std::ldexp(1.0, -pl->frac));
+    fp.partials    = pl->d_partials;
+    fp.nslices     = pl->nslices;
+    fp.status      = pl->d_status;
+    return nslots;
+  }
+
+  int item_prefix(rg_spectrum_plan* pl, const int64_t* d_off, int nseg, int64_t n, cudaStream_t s) {
+    item_prefix_kernel<<<1, 1024, 0, s>>>(d_off, nseg, n, pl->d_prefix, pl->d_status);
+    RG_CUDA_TRY(cudaGetLastError());
+    return RG_OK;
+  }
+
+  namespace {
 
     // Launches fused + reduce.  `d_off` (device, nseg + 1) may be null for a
     // single segment [0, n_single).  With `acc64` the spectra are added in FP64
     // to acc64 (nseg x nbins) instead of being written to `out`.
     int run_fused(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off,
-                  int64_t n_single, int nseg, float* out, cudaStream_t s,
-                  double* acc64 = nullptr) {
+                  int64_t n_single, int nseg, float* out, cudaStream_t s, double* acc64 = nullptr) {
       if (nseg <= 0 || pl->nbins == 0) {
         return RG_OK;
       }
@@ -865,42 +717,11 @@ namespace rg {
       RG_TRY(plan_reserve(pl, nseg));
       const int64_t* d_prefix = nullptr;
       if (d_off) {
-        item_prefix_kernel<<<1, 1024, 0, s>>>(d_off, nseg, n_single, pl->d_prefix, pl->d_status);
-        RG_CUDA_TRY(cudaGetLastError());
+        RG_TRY(item_prefix(pl, d_off, nseg, n_single, s));
         d_prefix = pl->d_prefix;
       }
-      FusedParams fp {};
-      int         nslots  = 0;
-      bool        aligned = true;
-      for (int c = 0; c < kComps; ++c) {
-        fp.comp[c] = comp[c];
-        fp.slot[c] = -1;
-        if (comp[c]) {
-          fp.slot[c] = nslots++;
-          aligned    = aligned && (reinterpret_cast<uintptr_t>(comp[c]) % 16 == 0);
-        }
-      }
-      fp.nslots      = nslots;
-      fp.use_tma     = aligned ? 1 : 0;
-      fp.source      = pl->source;
-      fp.has_e       = (comp[3] || comp[4] || comp[5]) ? 1 : 0;
-      fp.has_w       = comp[9] ? 1 : 0;
-      fp.log_spaced  = pl->log_spaced;
-      fp.seg_off     = d_off;
-      fp.item_prefix = d_prefix;
-      fp.n_single    = n_single;
-      fp.nseg        = nseg;
-      fp.P           = pl->d_P;
-      fp.Prange      = pl->d_Prange;
-      fp.L           = pl->L;
-      fp.Sh          = pl->Sh;
-      fp.Sl          = pl->Sl;
-      fp.Cfx         = pl->Cfx;
-      fp.amp         = pl->amp;
-      fp.table       = pl->ref->d_coef;
-      fp.partials    = pl->d_partials;
-      fp.nslices     = pl->nslices;
-      fp.status      = pl->d_status;
+      FusedParams fp;
+      const int   nslots = fill_params(pl, comp, d_off, d_prefix, n_single, nseg, fp);
       // a single segment with fewer items than blocks uses fewer blocks
       int G = pl->grid;
       if (!d_off) {
@@ -909,7 +730,7 @@ namespace rg {
       }
       const bool any = d_off ? true : n_single > 0;
       if (any) {
-        RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(nslots), s));
+        RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(pl->table_mode, kSmoothSegments, nslots), s));
       }
       ReduceParams rp {};
       rp.partials    = pl->d_partials;
@@ -927,22 +748,6 @@ namespace rg {
       dim3 rgrid((pl->nbins + 127) / 128, nseg);
       reduce_partials_kernel<<<rgrid, 128, 0, s>>>(rp);
       RG_CUDA_TRY(cudaGetLastError());
-      return RG_OK;
-    }
-
-    void particle_comps(const rg_particles* p, const float* out[kComps]) {
-      for (int d = 0; d < 3; ++d) {
-        out[d]     = p->u[d];
-        out[3 + d] = p->e[d];
-        out[6 + d] = p->b[d];
-      }
-      out[9] = p->w;
-    }
-
-    int check_particles(const rg_particles* p) {
-      if (!p || p->n < 0 || (p->n > 0 && (!p->u[0] || !p->u[1] || !p->u[2]))) {
-        return set_error(RG_ERR_ARGUMENT, "particles need U1..U3 device arrays and n >= 0");
-      }
       return RG_OK;
     }
 
@@ -964,8 +769,8 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
     return rg::set_error(RG_ERR_ARGUMENT, "null plan pointer");
   }
   *plan = nullptr;
-  if (table_mode != RG_TABLE_REFERENCE) {
-    return rg::set_error(RG_ERR_UNSUPPORTED, "table mode not available for this entry point");
+  if (table_mode != RG_TABLE_REFERENCE && table_mode != RG_TABLE_SMOOTH) {
+    return rg::set_error(RG_ERR_ARGUMENT, "unknown table mode");
   }
   if (B0 == 0.0f) {
     return rg::set_error(RG_ERR_ARGUMENT, "B0 must be non-zero");
@@ -987,8 +792,10 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
                     (static_cast<double>(g_syn) * g_syn * static_cast<double>(B0));
   pl->zero = !(K0 > 0.0) || !std::isfinite(K0);
   pl->amp  = static_cast<float>(1.0 / static_cast<double>(B0));
-  st       = rg::plan_prepare_bins(pl.get(), pl->ref->ln_xmin, pl->ref->dln, pl->ref->n,
-                                   pl->zero ? 0.0 : std::log(K0));
+  double ln_xmin, dln;
+  int    nseg;
+  rg::table_geometry(pl.get(), ln_xmin, dln, nseg);
+  st = rg::plan_prepare_bins(pl.get(), ln_xmin, dln, nseg, pl->zero ? 0.0 : std::log(K0));
   if (st == RG_OK) {
     st = rg::plan_reserve(pl.get(), 1);
   }
@@ -1016,10 +823,16 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_stage[1]);
   cudaFree(pl->d_acc64);
   for (int b = 0; b < 2; ++b) {
-    if (pl->copied[b]) cudaEventDestroy(pl->copied[b]);
-    if (pl->consumed[b]) cudaEventDestroy(pl->consumed[b]);
+    if (pl->copied[b]) {
+      cudaEventDestroy(pl->copied[b]);
+    }
+    if (pl->consumed[b]) {
+      cudaEventDestroy(pl->consumed[b]);
+    }
   }
-  if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
+  if (pl->copy_stream) {
+    cudaStreamDestroy(pl->copy_stream);
+  }
   for (auto* v : { &pl->ev_used, &pl->ev_free }) {
     for (auto& e : *v) {
       cudaEventDestroy(e.first);
@@ -1027,6 +840,34 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
     }
   }
   delete pl;
+  return RG_OK;
+}
+
+int rg_spectrum_plan_reserve(rg_spectrum_plan* pl, int32_t max_segments) {
+  if (!pl || max_segments < 1) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_reserve: bad arguments");
+  }
+  return rg::plan_reserve(pl, max_segments);
+}
+
+int rg_spectrum_plan_check(rg_spectrum_plan* pl, void* stream) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  auto     s  = static_cast<cudaStream_t>(stream);
+  unsigned st = 0;
+  RG_CUDA_TRY(cudaMemcpyAsync(&st, pl->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  RG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st != rg::kDevOk) {
+    RG_CUDA_TRY(cudaMemsetAsync(pl->d_status, 0, sizeof(unsigned), s));
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st & rg::kDevBadOffsets) {
+      return rg::set_error(RG_ERR_ARGUMENT,
+                           "segment offsets must be non-decreasing, >= 0 and <= the particle count");
+    }
+    return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait on the GPU gave up (status " + std::to_string(st) +
+                                           "); results are invalid");
+  }
   return RG_OK;
 }
 
@@ -1060,6 +901,31 @@ int rg_spectrum_plan_kernel_time(rg_spectrum_plan* pl, double* ms, int64_t* laun
   return RG_OK;
 }
 
+int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* out, void* stream) {
+  if (!plan || (!out && plan->nbins > 0)) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run: null argument");
+  }
+  if (plan->source != rg::kSrcParticles) {
+    return rg::set_error(RG_ERR_ARGUMENT, "plan was not made for particles");
+  }
+  RG_TRY(rg::check_particles(p));
+  const float* comp[rg::kComps];
+  rg::particle_comps(p, comp);
+  return rg::run_fused(const_cast<rg_spectrum_plan*>(plan), comp, nullptr, p->n, 1, out,
+                       static_cast<cudaStream_t>(stream));
+}
+
+int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
+                            int32_t nseg, float* out, void* stream) {
+  if (!plan || !offsets || nseg < 0 || (!out && nseg > 0 && plan->nbins > 0)) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_batched: null argument");
+  }
+  RG_TRY(rg::check_particles(p));
+  const float* comp[rg::kComps];
+  rg::particle_comps(p, comp);
+  return rg::run_fused(plan, comp, offsets, p->n, nseg, out, static_cast<cudaStream_t>(stream));
+}
+
 int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out, void* stream) {
   if (!pl || (!out && pl->nbins > 0) || pl->source != rg::kSrcParticles) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_host: bad arguments");
@@ -1068,7 +934,7 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
   if (pl->nbins == 0) {
     return RG_OK;
   }
-  auto s = static_cast<cudaStream_t>(stream);
+  auto              s           = static_cast<cudaStream_t>(stream);
   constexpr int64_t kStageChunk = int64_t(1) << 22; // particles per staged chunk
   if (!pl->d_stage[0]) {
     for (int b = 0; b < 2; ++b) {
@@ -1105,71 +971,17 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
     RG_TRY(rg::run_fused(pl, dev, nullptr, m, 1, out, s, pl->d_acc64));
     RG_CUDA_TRY(cudaEventRecord(pl->consumed[b], s));
   }
-  rg::finalize_acc_kernel<<<(pl->nbins + 255) / 256, 256, 0, s>>>(pl->d_acc64, pl->nbins,
-                                                                  pl->d_status, out);
+  rg::finalize_acc_kernel<<<(pl->nbins + 255) / 256, 256, 0, s>>>(pl->d_acc64, pl->nbins, pl->d_status,
+                                                                  out);
   RG_CUDA_TRY(cudaGetLastError());
   return RG_OK;
-}
-
-int rg_spectrum_plan_reserve(rg_spectrum_plan* pl, int32_t max_segments) {
-  if (!pl || max_segments < 1) {
-    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_reserve: bad arguments");
-  }
-  return rg::plan_reserve(pl, max_segments);
-}
-
-int rg_spectrum_plan_check(rg_spectrum_plan* pl, void* stream) {
-  if (!pl) {
-    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
-  }
-  auto     s  = static_cast<cudaStream_t>(stream);
-  unsigned st = 0;
-  RG_CUDA_TRY(cudaMemcpyAsync(&st, pl->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-  RG_CUDA_TRY(cudaStreamSynchronize(s));
-  if (st != rg::kDevOk) {
-    RG_CUDA_TRY(cudaMemsetAsync(pl->d_status, 0, sizeof(unsigned), s));
-    RG_CUDA_TRY(cudaStreamSynchronize(s));
-    if (st & rg::kDevBadOffsets) {
-      return rg::set_error(RG_ERR_ARGUMENT,
-                           "segment offsets must be non-decreasing, >= 0 and <= the particle count");
-    }
-    return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait on the GPU gave up (status " +
-                                           std::to_string(st) + "); results are invalid");
-  }
-  return RG_OK;
-}
-
-int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* out,
-                    void* stream) {
-  if (!plan || (!out && plan->nbins > 0)) {
-    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run: null argument");
-  }
-  if (plan->source != rg::kSrcParticles) {
-    return rg::set_error(RG_ERR_ARGUMENT, "plan was not made for particles");
-  }
-  RG_TRY(rg::check_particles(p));
-  const float* comp[rg::kComps];
-  rg::particle_comps(p, comp);
-  return rg::run_fused(const_cast<rg_spectrum_plan*>(plan), comp, nullptr, p->n, 1, out,
-                       static_cast<cudaStream_t>(stream));
-}
-
-int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p,
-                            const int64_t* offsets, int32_t nseg, float* out, void* stream) {
-  if (!plan || !offsets || nseg < 0 || (!out && nseg > 0 && plan->nbins > 0)) {
-    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_batched: null argument");
-  }
-  RG_TRY(rg::check_particles(p));
-  const float* comp[rg::kComps];
-  rg::particle_comps(p, comp);
-  return rg::run_fused(plan, comp, offsets, p->n, nseg, out, static_cast<cudaStream_t>(stream));
 }
 
 int rg_spectrum_run_plain(const rg_spectrum_plan* cplan, const rg_particles* p, float* out,
                           void* stream) {
   auto* plan = const_cast<rg_spectrum_plan*>(cplan);
-  if (!plan || plan->source != rg::kSrcParticles) {
-    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_plain: bad arguments");
+  if (!plan || plan->source != rg::kSrcParticles || plan->table_mode != RG_TABLE_REFERENCE) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_plain: needs a reference-table particle plan");
   }
   RG_TRY(rg::check_particles(p));
   auto s = static_cast<cudaStream_t>(stream);
@@ -1205,8 +1017,7 @@ int rg_spectrum_run_plain(const rg_spectrum_plan* cplan, const rg_particles* p, 
     return rg::set_error(RG_ERR_UNSUPPORTED, "plain kernel: too many bins");
   }
   if (smem > 48 * 1024) {
-    RG_CUDA_TRY(cudaFuncSetAttribute(rg::plain_spectrum_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RG_CUDA_TRY(cudaFuncSetAttribute(rg::plain_spectrum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));
   }
   if (p->n > 0) {
@@ -1215,8 +1026,7 @@ int rg_spectrum_run_plain(const rg_spectrum_plan* cplan, const rg_particles* p, 
     rg::plain_spectrum_kernel<<<blocks, 256, smem, s>>>(pp);
     RG_CUDA_TRY(cudaGetLastError());
   }
-  rg::f64_to_f32_kernel<<<(plan->nbins + 255) / 256, 256, 0, s>>>(plan->d_plain_acc, out,
-                                                                   plan->nbins);
+  rg::f64_to_f32_kernel<<<(plan->nbins + 255) / 256, 256, 0, s>>>(plan->d_plain_acc, out, plan->nbins);
   RG_CUDA_TRY(cudaGetLastError());
   return RG_OK;
 }
@@ -1237,8 +1047,7 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
     std::lock_guard<std::mutex> lock(rg::oneshot_mutex());
     auto                        it = cache.find(key);
     if (it == cache.end()) {
-      RG_TRY(rg_spectrum_plan_create(bins, nbins, B0, g_syn, e_syn_at_g_syn, RG_TABLE_REFERENCE,
-                                     &pl));
+      RG_TRY(rg_spectrum_plan_create(bins, nbins, B0, g_syn, e_syn_at_g_syn, RG_TABLE_REFERENCE, &pl));
       if (cache.size() >= 32) {
         RG_CUDA_TRY(cudaDeviceSynchronize());
         for (auto& kv : cache) {
@@ -1254,10 +1063,23 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
   return rg_spectrum_run(pl, p, out, stream);
 }
 
+int rg_dist_run(const rg_spectrum_plan* plan, const float* gbeta, const float* f, int32_t ng, float* out,
+                void* stream) {
+  if (!plan || plan->source != rg::kSrcDist || ng < 0 || (ng > 0 && (!gbeta || !f)) ||
+      (!out && plan->nbins > 0)) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_dist_run: bad arguments");
+  }
+  // the distribution source reads comp[0] = gbeta and comp[1] = f
+  const float* comp[rg::kComps] = {};
+  comp[0]                       = gbeta;
+  comp[1]                       = f;
+  return rg::run_fused(const_cast<rg_spectrum_plan*>(plan), comp, nullptr, ng, 1, out,
+                       static_cast<cudaStream_t>(stream));
+}
+
 int rg_synchrotron_spectrum_from_dist(const float* gbeta, const float* f, int32_t ng,
                                       int32_t log_spaced, const float* bins, int32_t nbins,
-                                      float g_syn, float e_syn_at_g_syn, float* out,
-                                      void* stream) {
+                                      float g_syn, float e_syn_at_g_syn, float* out, void* stream) {
   rg::clear_error();
   if (ng < 0 || nbins < 0 || (ng > 0 && (!gbeta || !f)) || (nbins > 0 && !out)) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_synchrotron_spectrum_from_dist: bad arguments");
@@ -1273,15 +1095,17 @@ int rg_synchrotron_spectrum_from_dist(const float* gbeta, const float* f, int32_
   pl->zero        = !(K0 > 0.0) || !std::isfinite(K0);
   pl->amp         = 1.0f;
   if (st == RG_OK) {
-    st = rg::plan_prepare_bins(pl.get(), pl->ref->ln_xmin, pl->ref->dln, pl->ref->n,
-                               pl->zero ? 0.0 : std::log(K0));
+    double ln_xmin, dln;
+    int    nseg;
+    rg::table_geometry(pl.get(), ln_xmin, dln, nseg);
+    st = rg::plan_prepare_bins(pl.get(), ln_xmin, dln, nseg, pl->zero ? 0.0 : std::log(K0));
   }
   auto s = static_cast<cudaStream_t>(stream);
   if (st == RG_OK) {
     const float* comp[rg::kComps] = {};
     comp[0]                       = gbeta;
     comp[1]                       = f;
-    st = rg::run_fused(pl.get(), comp, nullptr, ng, 1, out, s);
+    st                            = rg::run_fused(pl.get(), comp, nullptr, ng, 1, out, s);
   }
   if (st == RG_OK) {
     const cudaError_t e = cudaStreamSynchronize(s);

@@ -1,0 +1,262 @@
+// Device pieces shared by the spectrum forward (spectrum.cu) and adjoint
+// (adjoint.cu) kernels: launch geometry, parameters, the per-particle stage
+// (kinematics to a fixed-point table coordinate), work items and TMA staging.
+//
+// Reference: sync::Kernel<D>::OmegaSync_ChiR (synchrotron.hpp:181-232) for the
+// kinematics, InterpolateTabulatedFunction<true> (tabulation.hpp:19-53) for the
+// table coordinate, sync::KernelFromDist (synchrotron.hpp:72-95) for the
+// distribution source.
+#pragma once
+
+#include "rg_common.cuh"
+#include "rg_internal.hpp"
+
+namespace rg {
+
+  constexpr int kThreads     = 256;
+  constexpr int kWarps       = kThreads / 32;
+  constexpr int kSliceBins   = 512; // bins per block slice (K <= 16 rows of 32)
+  constexpr int kChunk       = 512; // particles per work item
+  constexpr int kChunkPad    = kChunk + 4;
+  constexpr int kComps       = 10;  // u0 u1 u2 e0 e1 e2 b0 b1 b2 w
+  constexpr int kBlocksPerSM = 2;
+
+  // extra status bit: segment offsets were not non-decreasing / within [0, n]
+  constexpr unsigned kDevBadOffsets = 4u;
+
+  enum Source : int { kSrcParticles = 0, kSrcDist = 1 };
+  enum Mode : int { kModeRef = RG_TABLE_REFERENCE, kModeSmooth = RG_TABLE_SMOOTH };
+
+  struct FusedParams {
+    const float*   comp[kComps]; // particle streams (dist: comp[0] = gbeta, comp[1] = f)
+    int            slot[kComps]; // shared-memory stream slot, -1 if not staged
+    int            nslots;
+    int            source;
+    int            has_e;
+    int            has_w;
+    int            use_tma;
+    int            log_spaced;   // dist: J_g = gbeta when set
+    const int64_t* seg_off;      // nseg + 1 particle offsets (device), or null: one segment
+    const int64_t* item_prefix;  // nseg + 1 cumulative item counts (device), or null
+    int64_t        n_single;     // particle count when seg_off is null
+    int            nseg;
+    const int32_t* P;            // nslices * kSliceBins fixed-point bin coordinates
+    const int64_t* Prange;       // per slice: (Pmin, Pmax) over valid bins
+    int64_t        L;            // table segments << frac
+    float          Sh, Sl;       // 2^frac / (2 dln) as a double-float
+    int64_t        Cfx;          // round(S ln2 2^16)
+    float          amp;          // 1 / B0 (particles) or 1 (dist)
+    // reference mode: 1024 (c0, c1 * 2^127) segments, frac = kFrac
+    const float2*  table;
+    // smooth mode: hseg Hermite segments + one zero entry, runtime frac
+    const float4*  htable;
+    int            hseg;
+    int            frac;
+    float          tau_scale;    // 2^-frac
+    double*        partials;     // [(grid + nseg) * nslices * kWarps * kSliceBins]
+    int            nslices;
+    unsigned*      status;
+  };
+
+  struct ItemInfo {
+    int     seg;
+    int     np;
+    int64_t pstart, pend, a0, a1;
+  };
+
+  __device__ __forceinline__ int64_t seg_begin(const FusedParams& p, int s) {
+    return p.seg_off ? p.seg_off[s] : 0;
+  }
+
+  __device__ __forceinline__ int64_t seg_end(const FusedParams& p, int s) {
+    return p.seg_off ? p.seg_off[s + 1] : p.n_single;
+  }
+
+  __device__ __forceinline__ int64_t items_before(const int64_t* prefix, int s) {
+    return prefix ? prefix[s] : 0;
+  }
+
+  __device__ __forceinline__ int64_t total_items(const int64_t* prefix, int nseg, int64_t n_single) {
+    return prefix ? prefix[nseg] : (n_single + kChunk - 1) / kChunk;
+  }
+
+  // Block b of G owns items [b n / G, (b+1) n / G); the block holding item i:
+  __device__ __forceinline__ int block_of_item(int64_t i, int64_t n_items, int G) {
+    return static_cast<int>(((i + 1) * G - 1) / n_items);
+  }
+
+  // ---- accurate logarithm of a positive double-float ---------------------------
+  struct LnParts {
+    int   e; // ln x = e ln2 + h + l
+    float h, l;
+  };
+
+  __device__ __forceinline__ LnParts ln_parts(ff x) {
+    int   e;
+    float m = frexpf(x.hi, &e); // x.hi = m 2^e, m in [0.5, 1)
+    if (m < 0.70710678f) {
+      m = __fmul_rn(m, 2.0f);
+      e -= 1;
+    }
+    // ln m = 2 atanh(z), z = (m - 1)/(m + 1), |z| < 0.1716
+    const float f  = __fsub_rn(m, 1.0f); // exact
+    const ff    d  = two_sum(m, 1.0f);
+    const float q  = __fdiv_rn(f, d.hi);
+    const float r  = __fmaf_rn(-q, d.hi, f); // exact remainder
+    const float zl = __fdiv_rn(__fmaf_rn(-q, d.lo, r), d.hi);
+    const float w  = __fmul_rn(q, q);
+    const float poly =
+      w * (0.33333334f + w * (0.2f + w * (0.14285715f + w * (0.11111111f + w * 0.09090909f))));
+    LnParts o;
+    o.e = e;
+    o.h = __fmul_rn(2.0f, q);
+    o.l = __fadd_rn(__fmaf_rn(o.h, poly, __fmul_rn(2.0f, zl)), __fdiv_rn(x.lo, x.hi));
+    return o;
+  }
+
+  // round(S (ln X1 + ln X2)), S = Sh + Sl; the exponent part goes through the
+  // integer constant Cfx = round(S ln2 2^16).
+  __device__ __forceinline__ int64_t fixed_log_sum(ff X1, ff X2, float Sh, float Sl, int64_t Cfx) {
+    const LnParts a = ln_parts(X1);
+    const LnParts b = ln_parts(X2);
+    ff            s = two_sum(a.h, b.h);
+    s.lo            = __fadd_rn(s.lo, __fadd_rn(a.l, b.l));
+    const float ph  = __fmul_rn(s.hi, Sh);
+    const float pe  = __fmaf_rn(s.hi, Sh, -ph);
+    const float pl  = __fadd_rn(pe, __fmaf_rn(s.hi, Sl, __fmul_rn(s.lo, Sh)));
+    const int64_t q = static_cast<int64_t>(a.e + b.e) * Cfx + __float2ll_rn(__fmul_rn(ph, 65536.0f)) +
+                      __float2ll_rn(__fmul_rn(pl, 65536.0f));
+    return (q + 32768) >> 16;
+  }
+
+  // gamma^2 = 1 + u^2 and W = |gamma E + u x B|^2 - (u.E)^2 as double-floats, so
+  // that chiR = sqrt(W) / (gamma B0) and e_peak = K0 gamma sqrt(W).
+  __device__ __forceinline__ void kinematics_ff(const float (&v)[kComps], bool has_e, ff& G, ff& W) {
+    const float ux = v[0], uy = v[1], uz = v[2];
+    const float bx = v[6], by = v[7], bz = v[8];
+    ff          u2 = two_prod(ux, ux);
+    u2             = ff_add(u2, two_prod(uy, uy));
+    u2             = ff_add(u2, two_prod(uz, uz));
+    G              = ff_add(ff { 1.0f, 0.0f }, u2);
+    const ff cx    = ff_diff_of_products(uy, bz, uz, by);
+    const ff cy    = ff_diff_of_products(uz, bx, ux, bz);
+    const ff cz    = ff_diff_of_products(ux, by, uy, bx);
+    if (!has_e) {
+      W = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
+    } else {
+      const float ex = v[3], ey = v[4], ez = v[5];
+      // gamma as a double-float: g = sqrt(G.hi), correction (G - g^2) / (2 g)
+      const float gh = sqrtf(G.hi);
+      const float gl = __fdiv_rn(__fadd_rn(__fmaf_rn(-gh, gh, G.hi), G.lo), __fmul_rn(2.0f, gh));
+      const ff    gm { gh, gl };
+      const ff    Vx = ff_add(ff_mul(gm, ff { ex, 0.0f }), cx);
+      const ff    Vy = ff_add(ff_mul(gm, ff { ey, 0.0f }), cy);
+      const ff    Vz = ff_add(ff_mul(gm, ff { ez, 0.0f }), cz);
+      ff          uE = two_prod(ux, ex);
+      uE             = ff_add(uE, two_prod(uy, ey));
+      uE             = ff_add(uE, two_prod(uz, ez));
+      W = ff_add(ff_add(ff_add(ff_sqr(Vx), ff_sqr(Vy)), ff_sqr(Vz)), ff_neg(ff_sqr(uE)));
+    }
+  }
+
+  // Per-particle stage for particle data.  Returns false if the particle adds
+  // nothing (e_peak <= 0 or not finite, or x outside the table for every bin).
+  __device__ __forceinline__ bool particle_stage(const float (&v)[kComps], const FusedParams& p,
+                                                 int64_t Pmin, int64_t Pmax, uint32_t& q32,
+                                                 float& A) {
+    ff G, W;
+    kinematics_ff(v, p.has_e != 0, G, W);
+    if (!(W.hi > 0.0f) || !isfinite(W.hi) || !isfinite(G.hi)) {
+      return false;
+    }
+    const int64_t Q = fixed_log_sum(G, W, p.Sh, p.Sl, p.Cfx);
+    if (Q <= Pmin - p.L || Q > Pmax) {
+      return false;
+    }
+    q32 = static_cast<uint32_t>(Q);
+    A   = p.amp * sqrtf(__fdiv_rn(W.hi, G.hi));
+    if (p.has_w) {
+      A *= v[9];
+    }
+    return isfinite(A);
+  }
+
+  // Per-"particle" stage of a tabulated distribution (synchrotron.hpp:76-94):
+  // e_peak = K0 gbeta^2, amplitude f * (gbeta if the gamma bins are log-spaced).
+  __device__ __forceinline__ bool dist_stage(float gb, float f, const FusedParams& p, int64_t Pmin,
+                                             int64_t Pmax, uint32_t& q32, float& A) {
+    const ff X = two_prod(gb, gb);
+    if (!(X.hi > 0.0f) || !isfinite(X.hi)) {
+      return false;
+    }
+    const int64_t Q = fixed_log_sum(X, X, p.Sh, p.Sl, p.Cfx);
+    if (Q <= Pmin - p.L || Q > Pmax) {
+      return false;
+    }
+    q32 = static_cast<uint32_t>(Q);
+    A   = p.log_spaced ? __fmul_rn(f, gb) : f;
+    return isfinite(A);
+  }
+
+  // Coordinate given to a particle that adds nothing: every bin lands past the
+  // last table segment (T - L in [0, R] for all bins), so it reads a zero entry.
+  __device__ __forceinline__ uint32_t dead_coordinate(int64_t Pmin, int64_t L) {
+    return static_cast<uint32_t>(Pmin - L);
+  }
+
+  __device__ __forceinline__ ItemInfo item_info(const FusedParams& p, int64_t i, int& seg_hint) {
+    int s = seg_hint;
+    while (s + 1 < p.nseg && items_before(p.item_prefix, s + 1) <= i) {
+      ++s;
+    }
+    seg_hint        = s;
+    const int64_t c = i - items_before(p.item_prefix, s);
+    ItemInfo      I;
+    I.seg    = s;
+    I.pstart = seg_begin(p, s) + c * kChunk;
+    I.pend   = min(I.pstart + kChunk, seg_end(p, s));
+    I.np     = static_cast<int>(I.pend - I.pstart);
+    I.a0     = I.pstart & ~int64_t(3);
+    I.a1     = I.pend & ~int64_t(3);
+    if (I.a1 < I.a0) {
+      I.a1 = I.a0;
+    }
+    return I;
+  }
+
+  // One elected thread: 1-D TMA bulk copies of the item's 16-byte-aligned span
+  // [a0, a1) of every staged stream into `buf`, completing on `bar`.
+  __device__ __forceinline__ void issue_stage(const FusedParams& p, const ItemInfo& I, float* buf,
+                                              uint64_t* bar) {
+    const uint32_t bytes = static_cast<uint32_t>(I.a1 - I.a0) * 4u;
+    mbar_arrive_expect_tx(bar, bytes * static_cast<uint32_t>(p.nslots));
+    if (bytes) {
+      for (int c = 0; c < kComps; ++c) {
+        if (p.slot[c] >= 0) {
+          bulk_g2s(buf + p.slot[c] * kChunkPad, p.comp[c] + I.a0, bytes, bar);
+        }
+      }
+    }
+  }
+
+  // Particle gp's components: from the staged span when present, else global.
+  __device__ __forceinline__ void load_comps(const FusedParams& p, const ItemInfo& I,
+                                             const float* sbuf, int64_t gp, float (&v)[kComps]) {
+    const bool in_smem = p.use_tma && gp < I.a1;
+#pragma unroll
+    for (int c = 0; c < kComps; ++c) {
+      const float* src = p.comp[c];
+      v[c]             = 0.0f;
+      if (src) {
+        v[c] = in_smem ? sbuf[p.slot[c] * kChunkPad + (gp - I.a0)] : __ldg(src + gp);
+      }
+    }
+  }
+
+  __device__ __forceinline__ double* warp_partial(const FusedParams& p, int b, int seg, int slice,
+                                                  int warp) {
+    return p.partials +
+           ((static_cast<int64_t>(b + seg) * p.nslices + slice) * kWarps + warp) * kSliceBins;
+  }
+
+} // namespace rg

@@ -1,0 +1,122 @@
+"""torch.autograd bindings of the synchrotron spectrum (thin layer over the C ABI).
+
+    import torch
+    from ragnar_gb300 import torch_ext as rt
+
+    plan = rt.spectrum_plan(bins, B0=1.0, g_syn=1.0, e_syn_at_g_syn=1.0)   # smooth table
+    S = rt.synchrotron_spectrum(plan, w, ux, uy, uz, bx, by, bz)          # [nbins]
+    loss = rt.log_mse(S, S_target)
+    loss.backward()                                                        # w.grad, ux.grad, ...
+
+The forward is the fused kernel (rg_spectrum_run); the backward is the
+hand-written adjoint kernel (rg_spectrum_adjoint), which recomputes e_peak
+instead of storing it.  With the smooth table (the default here) the derivative
+uses F'(x) = F(x)/x - x K_{5/3}(x).  All tensors are float32 on one CUDA device.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import capi
+
+
+def spectrum_plan(bins, B0: float = 1.0, g_syn: float = 1.0, e_syn_at_g_syn: float = 1.0,
+                  smooth: bool = True) -> capi.SpectrumPlan:
+    """Prepared spectrum over host photon energies `bins` (numpy/list/tensor)."""
+    if isinstance(bins, torch.Tensor):
+        bins = bins.detach().cpu().numpy()
+    mode = capi.RG_TABLE_SMOOTH if smooth else capi.RG_TABLE_REFERENCE
+    return capi.SpectrumPlan(np.asarray(bins, np.float32), B0, g_syn, e_syn_at_g_syn, mode)
+
+
+def dist_plan(bins, g_syn: float = 1.0, e_syn_at_g_syn: float = 1.0, log_spaced: bool = True,
+              smooth: bool = True) -> capi.DistPlan:
+    if isinstance(bins, torch.Tensor):
+        bins = bins.detach().cpu().numpy()
+    mode = capi.RG_TABLE_SMOOTH if smooth else capi.RG_TABLE_REFERENCE
+    return capi.DistPlan(np.asarray(bins, np.float32), g_syn, e_syn_at_g_syn, log_spaced, mode)
+
+
+def _check(t: torch.Tensor | None, name: str, dev) -> None:
+    if t is None:
+        return
+    if t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous float32 CUDA tensor")
+    if dev is not None and t.device != dev:
+        raise ValueError(f"{name} is on {t.device}, expected {dev}")
+
+
+def _stream(dev) -> int:
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+class _Spectrum(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan, w, ux, uy, uz, bx, by, bz, ex, ey, ez):  # noqa: PLR0913
+        dev = ux.device
+        for name, t in (("w", w), ("ux", ux), ("uy", uy), ("uz", uz), ("bx", bx), ("by", by),
+                        ("bz", bz), ("ex", ex), ("ey", ey), ("ez", ez)):
+            _check(t, name, dev)
+        e = None if ex is None else [ex, ey, ez]
+        prt = capi.particles([ux, uy, uz], b=[bx, by, bz], e=e, w=w, n=ux.numel())
+        out = torch.empty(plan.nbins, device=dev, dtype=torch.float32)
+        plan.run(prt, out, _stream(dev))
+        ctx.plan = plan
+        ctx.save_for_backward(w, ux, uy, uz, bx, by, bz, ex, ey, ez)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        w, ux, uy, uz, bx, by, bz, ex, ey, ez = ctx.saved_tensors
+        dev = ux.device
+        need_w, need_u = ctx.needs_input_grad[1], any(ctx.needs_input_grad[2:5])
+        gw = torch.empty_like(ux) if (need_w and w is not None) else None
+        gu = [torch.empty_like(ux) if ctx.needs_input_grad[2 + d] else None for d in range(3)]
+        if gw is None and not need_u:
+            return (None,) * 11
+        e = None if ex is None else [ex, ey, ez]
+        prt = capi.particles([ux, uy, uz], b=[bx, by, bz], e=e, w=w, n=ux.numel())
+        ctx.plan.adjoint(prt, grad_out.contiguous().float(), gw, gu, _stream(dev))
+        return (None, gw, gu[0], gu[1], gu[2], None, None, None, None, None, None)
+
+
+def synchrotron_spectrum(plan: capi.SpectrumPlan, w, ux, uy, uz, bx, by, bz, ex=None, ey=None, ez=None):
+    """Differentiable particle spectrum S[b] = e_b sum_p w_p chiR_p F(e_b / e_peak_p).
+
+    Gradients flow to w and ux, uy, uz.  `w` may be None (unit weights)."""
+    return _Spectrum.apply(plan, w, ux, uy, uz, bx, by, bz, ex, ey, ez)
+
+
+class _FromDist(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan, gbeta, f):
+        dev = f.device
+        _check(gbeta, "gbeta", dev)
+        _check(f, "f", dev)
+        out = torch.empty(plan.nbins, device=dev, dtype=torch.float32)
+        plan.run_dist(gbeta, f, out, _stream(dev))
+        ctx.plan = plan
+        ctx.save_for_backward(gbeta, f)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        gbeta, f = ctx.saved_tensors
+        gf = torch.empty_like(f)
+        ctx.plan.adjoint_dist(gbeta, f, grad_out.contiguous().float(), gf, _stream(f.device))
+        return None, None, gf
+
+
+def synchrotron_from_dist(plan: capi.DistPlan, gbeta, f):
+    """Differentiable spectrum of one tabulated distribution; gradients flow to f."""
+    return _FromDist.apply(plan, gbeta, f)
+
+
+def log_mse(S, S_target):
+    """mean over bins where both spectra are positive of (log S - log S_target)^2."""
+    m = (S > 0) & (S_target > 0)
+    d = torch.log(torch.where(m, S, torch.ones_like(S))) - torch.log(
+        torch.where(m, S_target, torch.ones_like(S_target)))
+    return (d * d * m).sum() / m.sum().clamp(min=1)
