@@ -505,11 +505,19 @@ namespace {
 
   // F(x) = x int_x^inf K_{5/3}(t) dt with t = x e^v (dt = t dv), v in [0, ln(60/x)],
   // 96 panels x 16-point Gauss-Legendre, K from std::cyl_bessel_k.
-  double exact_F_oracle(double x) {
-    static std::vector<double> gx, gw;
-    if (gx.empty()) {
-      gauss_legendre(16, gx, gw);
+  struct GaussLegendre16 {
+    std::vector<double> x, w;
+
+    GaussLegendre16() {
+      gauss_legendre(16, x, w);
     }
+  };
+
+  double exact_F_oracle(double x) {
+    // function-local static: initialised once, thread-safely, before first use
+    static const GaussLegendre16 gl;
+    const std::vector<double>&   gx = gl.x;
+    const std::vector<double>&   gw = gl.w;
     const double V = std::log(std::max(60.0, 2.0 * x) / x) + 1.0;
     const int    P = 96;
     double       s = 0.0;

@@ -114,9 +114,11 @@ def synchrotron_from_dist(plan: capi.DistPlan, gbeta, f):
     return _FromDist.apply(plan, gbeta, f)
 
 
-def log_mse(S, S_target):
-    """mean over bins where both spectra are positive of (log S - log S_target)^2."""
-    m = (S > 0) & (S_target > 0)
+def log_mse(S, S_target, floor: float = 1e-12):
+    """mean of (log S - log S_target)^2 over the bins where both spectra exceed
+    `floor` times their peak (bins with a vanishing spectrum are left out: their
+    1/S weight would overflow and carries no information)."""
+    m = (S > floor * S.detach().max()) & (S_target > floor * S_target.max())
     d = torch.log(torch.where(m, S, torch.ones_like(S))) - torch.log(
         torch.where(m, S_target, torch.ones_like(S_target)))
     return (d * d * m).sum() / m.sum().clamp(min=1)

@@ -34,9 +34,12 @@ def test_smooth_table_matches_independent_oracle(oracle_lib, smooth):
     coef, lnx, dln = smooth
     ref = oracle_lib.smooth_coefficients(coef.shape[0])
     assert abs(lnx - np.log(oracle_lib.SMOOTH_XMIN)) < 1e-15
-    # values and slopes of exact F from two independent FP64 quadratures, rounded to float
-    scale = np.abs(ref[:, 0:1]) + np.abs(ref[:, 1:2]) + 1e-300
-    assert np.max(np.abs(coef - ref) / scale) < 3e-7
+    # values and slopes of exact F from two independent FP64 quadratures, rounded to
+    # float; segments where F has fallen below float's normal range compare absolutely
+    scale = np.abs(ref[:, 0:1]) + np.abs(ref[:, 1:2])
+    big = scale[:, 0] > 1e-30
+    assert np.max(np.abs(coef[big] - ref[big]) / scale[big]) < 3e-7
+    assert np.max(np.abs(coef[~big] - ref[~big])) < 1e-36
 
 
 def _device(P, dev):
@@ -55,8 +58,9 @@ def test_smooth_forward(gpu, oracle_lib, smooth, nbins, lo, hi):
     assert max_rel(S.cpu().numpy(), truth) <= SPECTRUM_RTOL
 
 
-def _log_loss_np(S, St):
-    m = (S > 0) & (St > 0)
+def _log_loss_np(S, St, floor=1e-12):
+    # the loss of ragnar_gb300.torch_ext.log_mse: bins above floor x peak in both spectra
+    m = (S > floor * S.max()) & (St > floor * St.max())
     return np.sum((np.log(S[m]) - np.log(St[m])) ** 2) / m.sum(), m
 
 
@@ -109,7 +113,9 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
             fd = (vals[0] - vals[1]) / (2 * h)
             ref = max(abs(fd), 1e-3 * scale[c, 0])
             worst = max(worst, abs(g_gpu[c, p] - fd) / ref)
-            assert abs(g64[c, p] - fd) <= 1e-6 * ref + 1e-12, (p, key)
+            # the FP64 gradient itself against FD: the table is C1 (piecewise cubic), so a
+            # central difference straddling a segment joint is off by O(h |jump of F''|)
+            assert abs(g64[c, p] - fd) <= 1e-5 * ref + 1e-12, (p, key)
     assert worst < 1e-4, worst
 
 
