@@ -181,6 +181,21 @@ int rg_spectrum_run_plain(const rg_spectrum_plan* plan, const rg_particles* p, f
 int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nbins, float B0,
                             float g_syn, float e_syn_at_g_syn, float* out, void* stream);
 
+/* Allocation-free form of rg_synchrotron_spectrum, for callers that cannot
+ * allocate device memory once they run (a process that hands its whole device
+ * memory budget out at start-up, or a plugin inside one).  No counterpart in the
+ * reference.  Same arguments and result (reference table); every byte of scratch
+ * comes from one fixed file-scope device array of about 10.6 MB that each GPU
+ * loading the library keeps until exit, and the call makes no cudaMalloc,
+ * cudaFree or other allocating call.  At most 512 photon bins (larger counts are
+ * rejected with RG_ERR_ARGUMENT).  The first call on a device looks up the
+ * array's address and builds the F table into it, synchronising the device's
+ * default stream: make it before any stream capture.  All calls share the
+ * array: calls whose GPU work overlaps race on it.  A device-side failure shows
+ * as NaN outputs. */
+int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, int32_t nbins, float B0,
+                                    float g_syn, float e_syn_at_g_syn, float* out, void* stream);
+
 /* --------------------------------------------------------------------------
  * Adjoint (differentiation)
  * ------------------------------------------------------------------------ */

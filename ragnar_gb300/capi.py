@@ -86,6 +86,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_plan_enable_timing": [_vp, _i32],
         "rg_spectrum_plan_kernel_time": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64)],
         "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
+        "rg_synchrotron_spectrum_noalloc": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp,
+                                            _vp],
         "rg_synchrotron_spectrum_from_dist": [_vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _vp, _vp],
         "rg_spectrum_adjoint": [_vp, ctypes.POINTER(Particles), _vp, _vp, _vp, _vp, _vp, _vp],
         "rg_spectrum_adjoint_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp, _vp, _vp,

@@ -13,6 +13,7 @@
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -213,6 +214,33 @@ namespace rg {
     RG_CUDA_TRY(cudaGetLastError());
     t.h_y.resize(n);
     RG_CUDA_TRY(cudaMemcpyAsync(t.h_y.data(), t.d_y, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    RG_CUDA_TRY(cudaStreamSynchronize(s));
+    return RG_OK;
+  }
+
+  // The reference table built into caller-supplied device buffers (x, y: n floats;
+  // coef: kRefEntries float2; grids: n * 100 floats) without allocating; used by
+  // the allocation-free spectrum.  Synchronises `s`.
+  int build_reference_table_into(int n, float xmin, float xmax, float* d_x, float* d_y, float2* d_coef,
+                                 float* d_grids, double& ln_xmin, double& dln, cudaStream_t s) {
+    if (n < 2) {
+      return set_error(RG_ERR_ARGUMENT, "TabulateFfunc needs at least 2 points");
+    }
+    std::vector<float> hx(n);
+    for (int i = 0; i < n; ++i) {
+      hx[i] = logspace_point(xmin, xmax, static_cast<std::size_t>(n), static_cast<std::size_t>(i));
+    }
+    const float lo = *std::min_element(hx.begin(), hx.end());
+    const float hi = *std::max_element(hx.begin(), hx.end());
+    ln_xmin        = std::log(static_cast<double>(lo));
+    dln            = std::log(static_cast<double>(hi) / static_cast<double>(lo)) / (n - 1);
+    const std::vector<float> grids = inner_grids(hx);
+    RG_CUDA_TRY(cudaMemcpyAsync(d_x, hx.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    RG_CUDA_TRY(cudaMemcpyAsync(d_grids, grids.data(), sizeof(float) * grids.size(), cudaMemcpyHostToDevice, s));
+    ffunc_integrand_kernel<<<(n + 3) / 4, 128, 0, s>>>(d_x, d_grids, n, d_y, 1);
+    RG_CUDA_TRY(cudaGetLastError());
+    ref_coef_kernel<<<kRefEntries / 256, 256, 0, s>>>(d_x, d_y, n, ln_xmin, dln, d_coef);
+    RG_CUDA_TRY(cudaGetLastError());
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     return RG_OK;
   }

@@ -692,6 +692,34 @@ namespace rg {
     return nslots;
   }
 
+  // Launch entry points for callers that supply every device buffer themselves
+  // (the allocation-free spectrum in noalloc.cu): the reference-table fused
+  // kernel over one segment, and the block/warp reduction into `out`.
+  int launch_fused_reference(int K, const FusedParams& fp, int grid, cudaStream_t s) {
+    RG_CUDA_TRY(launch_fused_mode<kModeRef>(K, fp, dim3(grid, 1), fused_smem(kModeRef, 0, fp.nslots), s));
+    return RG_OK;
+  }
+
+  int launch_reduce_single(const double* partials, int grid, int64_t n, int nbins, const float* ebins,
+                           const uint8_t* valid, const unsigned* status, float* out, cudaStream_t s) {
+    ReduceParams rp {};
+    rp.partials    = partials;
+    rp.item_prefix = nullptr;
+    rp.n_single    = n;
+    rp.grid        = grid;
+    rp.nslices     = 1;
+    rp.nseg        = 1;
+    rp.nbins       = nbins;
+    rp.ebins       = ebins;
+    rp.valid       = valid;
+    rp.status      = status;
+    rp.out         = out;
+    rp.acc64       = nullptr;
+    reduce_partials_kernel<<<dim3((nbins + 127) / 128, 1), 128, 0, s>>>(rp);
+    RG_CUDA_TRY(cudaGetLastError());
+    return RG_OK;
+  }
+
   int item_prefix(rg_spectrum_plan* pl, const int64_t* d_off, int nseg, int64_t n, cudaStream_t s) {
     item_prefix_kernel<<<1, 1024, 0, s>>>(d_off, nseg, n, pl->d_prefix, pl->d_status);
     RG_CUDA_TRY(cudaGetLastError());
