@@ -244,6 +244,38 @@ int rg_synchrotron_spectrum_from_dist(const float* gbeta, const float* f, int32_
                                       void* stream);
 
 /* --------------------------------------------------------------------------
+ * Many distributions at once on the tensor cores
+ * ------------------------------------------------------------------------ */
+
+typedef struct rg_fromdist_plan rg_fromdist_plan;
+
+/* Batched SynchrotronSpectrumFromDist (synchrotron.cpp:69-105 once per
+ * distribution): up to max_dist distributions f[d][g] on the shared gamma bins
+ * gbeta (host, ng) give S[d][e] = e * sum_g K[e][g] f[d][g] with the kernel
+ * matrix K[e][g] = J_g F(e / e_peak(g)) (built once here, FP64).  The product
+ * runs as one BF16 tensor-core GEMM (tcgen05) over split-precision operands:
+ * split_products = 6 (three BF16 terms per operand, ~1e-8 relative) or 3 (two
+ * terms, ~1e-5 relative).  bins is host (nbins).  Either table mode.
+ * Extension: the reference handles one distribution per call. */
+int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, const float* bins, int32_t nbins,
+                            float g_syn, float e_syn_at_g_syn, int32_t table_mode, int32_t split_products,
+                            int32_t max_dist, rg_fromdist_plan** plan);
+int rg_fromdist_plan_destroy(rg_fromdist_plan* plan);
+
+/* f: device [ndist x ng] row-major; out: device [ndist x nbins]. */
+int rg_fromdist_run(rg_fromdist_plan* plan, const float* f, int32_t ndist, float* out, void* stream);
+
+/* Transpose GEMM: grad_f[d][g] = sum_e grad_out[d][e] e K[e][g] (device arrays). */
+int rg_fromdist_adjoint(rg_fromdist_plan* plan, const float* grad_out, int32_t ndist, float* grad_f,
+                        void* stream);
+
+/* Synchronises `stream`; RG_ERR_TIMEOUT if a bounded wait in the GEMM gave up. */
+int rg_fromdist_plan_check(rg_fromdist_plan* plan, void* stream);
+
+/* Copies the FP64 kernel matrix K (nbins x ng) to host memory. */
+int rg_fromdist_kernel_matrix(rg_fromdist_plan* plan, double* K_host);
+
+/* --------------------------------------------------------------------------
  * Energy distribution (histogram)
  * ------------------------------------------------------------------------ */
 

@@ -95,6 +95,13 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_dist_plan_create": [_vp, _i32, _f32, _f32, _i32, _i32, ctypes.POINTER(_vp)],
         "rg_dist_run": [_vp, _vp, _vp, _i32, _vp, _vp],
         "rg_dist_adjoint": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
+        "rg_fromdist_plan_create": [_vp, _i32, _i32, _vp, _i32, _f32, _f32, _i32, _i32, _i32,
+                                    ctypes.POINTER(_vp)],
+        "rg_fromdist_plan_destroy": [_vp],
+        "rg_fromdist_run": [_vp, _vp, _i32, _vp, _vp],
+        "rg_fromdist_adjoint": [_vp, _vp, _i32, _vp, _vp],
+        "rg_fromdist_plan_check": [_vp, _vp],
+        "rg_fromdist_kernel_matrix": [_vp, _vp],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
         "rg_smooth_table": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
                             ctypes.POINTER(ctypes.c_double)],
@@ -252,3 +259,47 @@ class DistPlan(SpectrumPlan):
     def adjoint_dist(self, gbeta, f, grad_out, grad_f, stream: int = 0) -> None:
         check(lib().rg_dist_adjoint(self.handle, addr(gbeta), addr(f), int(f.numel()), addr(grad_out),
                                     addr(grad_f), stream))
+
+
+class FromDistPlan:
+    """rg_fromdist_plan: many distributions on shared gamma bins via the tensor-core GEMM."""
+
+    def __init__(self, gbeta, log_spaced: bool, bins, g_syn: float, eps: float, max_dist: int,
+                 mode: int = RG_TABLE_REFERENCE, split_products: int = 6):
+        import numpy as np  # noqa: PLC0415
+
+        self.gbeta = np.ascontiguousarray(gbeta, dtype=np.float32)
+        self.bins = np.ascontiguousarray(bins, dtype=np.float32)
+        self.ng, self.nbins, self.max_dist = len(self.gbeta), len(self.bins), max_dist
+        h = _vp()
+        check(lib().rg_fromdist_plan_create(self.gbeta.ctypes.data, self.ng, int(log_spaced),
+                                            self.bins.ctypes.data, self.nbins, g_syn, eps, mode,
+                                            split_products, max_dist, ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, f, out, stream: int = 0) -> None:
+        check(lib().rg_fromdist_run(self.handle, addr(f), int(f.shape[0]), addr(out), stream))
+
+    def adjoint(self, grad_out, grad_f, stream: int = 0) -> None:
+        check(lib().rg_fromdist_adjoint(self.handle, addr(grad_out), int(grad_out.shape[0]), addr(grad_f), stream))
+
+    def check(self, stream: int = 0) -> None:
+        check(lib().rg_fromdist_plan_check(self.handle, stream))
+
+    def kernel_matrix(self):
+        import numpy as np  # noqa: PLC0415
+
+        K = np.empty((self.nbins, self.ng), np.float64)
+        check(lib().rg_fromdist_kernel_matrix(self.handle, K.ctypes.data))
+        return K
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().rg_fromdist_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # noqa: D105
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

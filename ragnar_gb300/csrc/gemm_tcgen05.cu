@@ -1,0 +1,629 @@
+// Batched SynchrotronSpectrumFromDist on the Blackwell tensor cores (sm_103a).
+//
+// Reference: SynchrotronSpectrumFromDist (synchrotron.cpp:69-105) evaluates, per
+// distribution, S[e] = sum_g f_g e J_g F(e / e_peak(g)) (synchrotron.hpp:72-95),
+// J_g = gbeta_g for log-spaced gamma bins, e_peak(g) = eps gbeta_g^2 / g_syn^2.
+// The kernel matrix K[e, g] = J_g F(e / e_peak(g)) depends only on the bins, so
+// many distributions f[d, g] give one GEMM:  S[d, e] = e * sum_g f[d, g] K[e, g].
+//
+// Precision: FP32 operands are split into BF16 terms (x = h + m + l, each the
+// BF16 rounding of the remainder) and the products are summed in one GEMM over
+// a concatenated K dimension, accumulated in FP32 in tensor memory:
+//   6 products  (h.h + h.m + m.h + h.l + l.h + m.m): ~1e-8 relative (default)
+//   3 products  (h.h + h.m + m.h):                  ~1e-5 relative (fast)
+//
+// GEMM: C[M x N] = A[M x K'] . B[N x K']^T, both operands K-major BF16.  CTA tile
+// 128 x 256, K step 64; TMA (cp.async.bulk.tensor, 128-byte swizzle) fills a
+// 4-stage shared-memory ring; one thread issues tcgen05.mma (M 128, N 256, K 16)
+// into a 128 x 256 FP32 accumulator in tensor memory and commits each stage
+// back to the producer; after the last commit all four warps read the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
+// C * col_scale.  Every mbarrier wait is bounded; a wait that gives up records
+// the status word, and the CTA still frees its tensor memory.
+#include "rg_common.cuh"
+#include "rg_internal.hpp"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+namespace rg {
+
+  namespace {
+
+    constexpr int kBM       = 128;
+    constexpr int kBN       = 256;
+    constexpr int kBK       = 64; // bf16 elements = 128 bytes: one swizzle row
+    constexpr int kStages   = 4;
+    constexpr int kUmmaK    = 16;
+    constexpr int kGemmThreads = 128;
+    constexpr uint32_t kBytesA = kBM * kBK * 2;
+    constexpr uint32_t kBytesB = kBN * kBK * 2;
+    constexpr uint32_t kTmemCols = 256;
+    constexpr unsigned kDevGemmTimeout = 8u;
+
+    __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y,
+                                                uint64_t* bar) {
+      asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+    }
+
+    // Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle
+    // layout: 8-row atoms of 128-byte rows, atoms 1024 bytes apart (SBO), the
+    // leading offset unused for swizzled K-major layouts (encoded 1).
+    __device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
+      const uint64_t addr = smem_u32(p);
+      uint64_t       d    = (addr & 0x3FFFFull) >> 4;
+      d |= uint64_t(1) << 16;           // leading byte offset (unused), encoded 16 >> 4
+      d |= uint64_t(1024 >> 4) << 32;   // stride byte offset: 8 rows x 128 B
+      d |= uint64_t(1) << 46;           // descriptor version for tcgen05
+      d |= uint64_t(2) << 61;           // swizzle: 128 B
+      return d;
+    }
+
+    // Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major,
+    // N = 256, M = 128.
+    constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kBN >> 3) << 17) |
+                                (uint32_t(kBM >> 4) << 24);
+
+    __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+      asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+    }
+
+    __device__ __forceinline__ void mma_commit(uint64_t* bar) {
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                   : "memory");
+    }
+
+    __device__ __forceinline__ void tc_fence_after() {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+
+    __device__ __forceinline__ void tc_fence_before() {
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+
+    // 32 consecutive FP32 columns of this thread's TMEM lane.
+    __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+      uint32_t r[32];
+      asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+        "[%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        v[i] = __uint_as_float(r[i]);
+      }
+    }
+
+    struct GemmArgs {
+      int          M, N, Kp; // Kp: concatenated K, a multiple of kBK
+      float*       C;
+      int          ldc;
+      const float* col_scale; // nullable
+      unsigned*    status;
+    };
+
+    __global__ void __launch_bounds__(kGemmThreads, 1)
+      gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                          const __grid_constant__ GemmArgs g) {
+      extern __shared__ __align__(1024) unsigned char smem_raw[];
+      // 1024-byte alignment of the swizzled stage buffers
+      unsigned char* smem = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+      unsigned char* sA = smem;
+      unsigned char* sB = smem + kStages * kBytesA;
+      __shared__ uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
+      __shared__ uint32_t tmem_slot;
+
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
+      const int nk = g.Kp / kBK;
+
+      if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+          mbar_init(&full_bar[s], 1);
+          mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&done_bar, 1);
+        fence_mbar_init();
+      }
+      if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+      }
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      const uint32_t tmem_d = tmem_slot;
+
+      int issued = 0; // k blocks the producer handed to TMA
+      if (warp == 0 && lane == 0) {
+        // ---- producer: TMA into the ring --------------------------------------------
+        for (int kb = 0; kb < nk; ++kb, ++issued) {
+          const int      s  = kb % kStages;
+          const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
+          if (kb >= kStages && !mbar_wait_bounded(&empty_bar[s], ph ^ 1u)) {
+            atomicOr(g.status, kDevGemmTimeout);
+            break;
+          }
+          mbar_arrive_expect_tx(&full_bar[s], kBytesA + kBytesB);
+          tma_load_2d(sA + s * kBytesA, &tmA, kb * kBK, m0, &full_bar[s]);
+          tma_load_2d(sB + s * kBytesB, &tmB, kb * kBK, n0, &full_bar[s]);
+        }
+      } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----------------------------------------------------------------
+        bool ok = true;
+        for (int kb = 0; kb < nk && ok; ++kb) {
+          const int      s  = kb % kStages;
+          const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
+          if (!mbar_wait_bounded(&full_bar[s], ph)) {
+            atomicOr(g.status, kDevGemmTimeout);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t da = smem_desc_sw128(sA + s * kBytesA);
+          const uint64_t db = smem_desc_sw128(sB + s * kBytesB);
+#pragma unroll
+          for (int k = 0; k < kBK / kUmmaK; ++k) {
+            // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
+            mma_bf16(tmem_d, da + uint64_t(2 * k), db + uint64_t(2 * k), (kb > 0 || k > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        mma_commit(&done_bar);
+      }
+      __syncwarp();
+
+      // ---- epilogue: TMEM -> registers -> global ---------------------------------------
+      // tcgen05.ld is warp-collective: every thread takes the same branch
+      const bool done = __syncthreads_and(mbar_wait_bounded(&done_bar, 0)) != 0;
+      if (!done && threadIdx.x == 0) {
+        atomicOr(g.status, kDevGemmTimeout);
+        // a wait gave up: let the copies still in flight land before the CTA exits
+        for (int s = 0; s < kStages && s < issued; ++s) {
+          const int last = s + ((issued - 1 - s) / kStages) * kStages;
+          mbar_wait_bounded(&full_bar[s], static_cast<uint32_t>(last / kStages) & 1u);
+        }
+      }
+      tc_fence_after();
+      if (done && nk > 0) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c = 0; c < kBN / 32; ++c) {
+          float v[32];
+          tmem_ld32(tmem_d + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c * 32), v);
+          const int col0 = n0 + c * 32;
+          if (row < g.M && col0 < g.N) {
+            float* dst = g.C + static_cast<int64_t>(row) * g.ldc + col0;
+            if (g.col_scale) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                v[j] *= (col0 + j < g.N) ? __ldg(g.col_scale + col0 + j) : 0.0f;
+              }
+            }
+            if (col0 + 32 <= g.N && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll
+              for (int j = 0; j < 32; j += 4) {
+                *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                if (col0 + j < g.N) {
+                  dst[j] = v[j];
+                }
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+      if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(kTmemCols)
+                     : "memory");
+      }
+    }
+
+    // ---- operand preparation -------------------------------------------------------------
+
+    // Splits v into BF16 terms h, m, l (each the rounding of the remainder).
+    __device__ __forceinline__ void split3(double v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+      h         = __double2bfloat16(v);
+      double r  = v - static_cast<double>(__bfloat162float(h));
+      m         = __double2bfloat16(r);
+      r        -= static_cast<double>(__bfloat162float(m));
+      l         = __double2bfloat16(r);
+    }
+
+    // dst[r][t * cpad + c] = term pattern[t] of src[r][c] * scale[c] (zero in the
+    // padding).  which = 0: left operand pattern, 1: right operand pattern.
+    __global__ void split_rows_kernel(const float* __restrict__ src, int rows, int cols, int ld,
+                                      const float* __restrict__ col_scale, __nv_bfloat16* __restrict__ dst,
+                                      int cpad, int nterms, int which) {
+      const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i >= static_cast<int64_t>(rows) * cpad) {
+        return;
+      }
+      const int r = static_cast<int>(i / cpad), c = static_cast<int>(i % cpad);
+      __nv_bfloat16 t[3];
+      if (c < cols) {
+        double v = src[static_cast<int64_t>(r) * ld + c];
+        if (col_scale) {
+          v *= static_cast<double>(col_scale[c]);
+        }
+        split3(v, t[0], t[1], t[2]);
+      } else {
+        t[0] = t[1] = t[2] = __float2bfloat16(0.0f);
+      }
+      // products (h,h) (h,m) (m,h) (h,l) (l,h) (m,m): left [h h m h l m], right [h m h l h m]
+      constexpr int left[6]  = { 0, 0, 1, 0, 2, 1 };
+      constexpr int right[6] = { 0, 1, 0, 2, 0, 1 };
+      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nterms * cpad;
+      for (int k = 0; k < nterms; ++k) {
+        row[k * cpad + c] = t[which ? right[k] : left[k]];
+      }
+    }
+
+    // Kernel matrix in FP64: K[e][g] = J_g F(e_b / e_peak(g)) with the plan's table,
+    // written as the right operand (rows e) and its transpose (rows g).
+    struct KParams {
+      const float*   gbeta; // ng
+      const float*   ebins; // nbins
+      int            ng, nbins, log_spaced;
+      double         ln_k0, ln_xmin, dln;
+      int            mode, nseg;
+      const float2*  ref;   // reference segments (c0, c1 * 2^127)
+      const float4*  hcoef; // smooth segments
+      double*        K;     // nbins x ng
+    };
+
+    __global__ void kernel_matrix_kernel(const __grid_constant__ KParams p) {
+      const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i >= static_cast<int64_t>(p.nbins) * p.ng) {
+        return;
+      }
+      const int    e = static_cast<int>(i / p.ng), g = static_cast<int>(i % p.ng);
+      const double gb = p.gbeta[g], eb = p.ebins[e];
+      double       K  = 0.0;
+      if (gb != 0.0 && eb > 0.0 && isfinite(gb) && isfinite(eb)) {
+        const double t = (log(eb) - p.ln_k0 - 2.0 * log(fabs(gb)) - p.ln_xmin) / p.dln;
+        if (t >= 0.0 && t < static_cast<double>(p.nseg)) {
+          const int    j   = static_cast<int>(t);
+          const double tau = t - j;
+          double       F;
+          if (p.mode == RG_TABLE_REFERENCE) {
+            const float2 c = p.ref[j];
+            F              = static_cast<double>(c.x) + tau * static_cast<double>(c.y) / kSlopeScale;
+          } else {
+            const float4 c = p.hcoef[j];
+            F = c.x + tau * (c.y + tau * (c.z + tau * static_cast<double>(c.w)));
+          }
+          K = F * (p.log_spaced ? gb : 1.0);
+        }
+      }
+      p.K[i] = K;
+    }
+
+    __global__ void split_matrix_kernel(const double* __restrict__ K, int nbins, int ng, int transpose,
+                                        __nv_bfloat16* __restrict__ dst, int cpad, int nterms) {
+      // rows: e (cols g) or, transposed, g (cols e)
+      const int     rows = transpose ? ng : nbins, cols = transpose ? nbins : ng;
+      const int64_t i    = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i >= static_cast<int64_t>(rows) * cpad) {
+        return;
+      }
+      const int r = static_cast<int>(i / cpad), c = static_cast<int>(i % cpad);
+      __nv_bfloat16 t[3];
+      if (c < cols) {
+        const double v = transpose ? K[static_cast<int64_t>(c) * ng + r] : K[static_cast<int64_t>(r) * ng + c];
+        split3(v, t[0], t[1], t[2]);
+      } else {
+        t[0] = t[1] = t[2] = __float2bfloat16(0.0f);
+      }
+      constexpr int right[6] = { 0, 1, 0, 2, 0, 1 };
+      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nterms * cpad;
+      for (int k = 0; k < nterms; ++k) {
+        row[k * cpad + c] = t[right[k]];
+      }
+    }
+
+    // ---- tensor maps -------------------------------------------------------------------------
+    using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                       const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                       CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                       CUtensorMapFloatOOBfill);
+
+    int encode_tiled(CUtensorMap* tm, void* base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
+      static EncodeTiledFn fn = nullptr;
+      if (!fn) {
+        void*                           p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        RG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (!p || q != cudaDriverEntryPointSuccess) {
+          return set_error(RG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        }
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+      }
+      const cuuint64_t dims[2]    = { cols, rows };
+      const cuuint64_t strides[1] = { cols * 2 };
+      const cuuint32_t box[2]     = { static_cast<cuuint32_t>(kBK), box_rows };
+      const cuuint32_t estr[2]    = { 1, 1 };
+      const CUresult   r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) {
+        return set_error(RG_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(static_cast<int>(r)) + ")");
+      }
+      return RG_OK;
+    }
+
+    size_t gemm_smem() {
+      return kStages * (kBytesA + kBytesB) + 1024;
+    }
+
+    int launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+      static bool configured = false;
+      if (!configured) {
+        RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(gemm_smem())));
+        configured = true;
+      }
+      if (g.M <= 0 || g.N <= 0) {
+        return RG_OK;
+      }
+      const dim3 grid((g.N + kBN - 1) / kBN, (g.M + kBM - 1) / kBM);
+      gemm_bf16_tn_kernel<<<grid, kGemmThreads, gemm_smem(), s>>>(tA, tB, g);
+      RG_CUDA_TRY(cudaGetLastError());
+      return RG_OK;
+    }
+
+    int round_up(int v, int m) {
+      return (v + m - 1) / m * m;
+    }
+
+  } // namespace
+
+} // namespace rg
+
+struct rg_fromdist_plan {
+  int            ng = 0, nbins = 0, nterms = 6, max_dist = 0, log_spaced = 1, mode = RG_TABLE_REFERENCE;
+  int            gpad = 0, epad = 0; // padded K extents of the forward / adjoint GEMMs
+  float          g_syn = 1, eps = 1;
+  bool           zero  = false;
+  float*         d_gbeta = nullptr;
+  float*         d_ebins = nullptr; // photon energies with invalid bins set to 0
+  double*        d_K     = nullptr; // nbins x ng kernel matrix (FP64)
+  __nv_bfloat16* d_B     = nullptr; // forward right operand  [nbins x nterms*gpad]
+  __nv_bfloat16* d_BT    = nullptr; // adjoint right operand  [ng x nterms*epad]
+  __nv_bfloat16* d_A     = nullptr; // forward left operand   [max_dist x nterms*gpad]
+  __nv_bfloat16* d_AT    = nullptr; // adjoint left operand   [max_dist x nterms*epad]
+  unsigned*      d_status = nullptr;
+  CUtensorMap    tA, tB, tAT, tBT;
+};
+
+extern "C" {
+
+int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, const float* bins, int32_t nbins,
+                            float g_syn, float e_syn_at_g_syn, int32_t table_mode, int32_t split_products,
+                            int32_t max_dist, rg_fromdist_plan** plan) {
+  rg::clear_error();
+  if (!plan || ng < 1 || nbins < 1 || max_dist < 1 || !gbeta || !bins) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_plan_create: bad arguments");
+  }
+  if (split_products != 3 && split_products != 6) {
+    return rg::set_error(RG_ERR_ARGUMENT, "split_products must be 3 or 6");
+  }
+  if (table_mode != RG_TABLE_REFERENCE && table_mode != RG_TABLE_SMOOTH) {
+    return rg::set_error(RG_ERR_ARGUMENT, "unknown table mode");
+  }
+  *plan          = nullptr;
+  auto pl        = std::make_unique<rg_fromdist_plan>();
+  pl->ng         = ng;
+  pl->nbins      = nbins;
+  pl->nterms     = split_products;
+  pl->max_dist   = max_dist;
+  pl->log_spaced = log_spaced ? 1 : 0;
+  pl->mode       = table_mode;
+  pl->g_syn      = g_syn;
+  pl->eps        = e_syn_at_g_syn;
+  pl->gpad       = rg::round_up(ng, rg::kBK);
+  pl->epad       = rg::round_up(nbins, rg::kBK);
+  const double K0 = static_cast<double>(e_syn_at_g_syn) / (static_cast<double>(g_syn) * g_syn);
+  pl->zero        = !(K0 > 0.0) || !std::isfinite(K0);
+
+  const rg::RefTable*    ref = nullptr;
+  const rg::SmoothTable* sm  = nullptr;
+  RG_TRY(rg::reference_table(&ref));
+  if (table_mode == RG_TABLE_SMOOTH) {
+    RG_TRY(rg::smooth_table(&sm));
+  }
+  std::vector<float> eb(bins, bins + nbins);
+  for (float& v : eb) {
+    if (!(v > 0.0f) || !std::isfinite(v)) {
+      v = 0.0f; // non-positive bins yield 0, as in the particle path
+    }
+  }
+  auto fail = [&](int st) {
+    rg_fromdist_plan_destroy(pl.release());
+    return st;
+  };
+#define RG_PLAN_CUDA(expr)                                                                  \
+  do {                                                                                      \
+    cudaError_t e_ = (expr);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      return fail(rg::cuda_error(e_, #expr));                                               \
+    }                                                                                       \
+  } while (0)
+  const size_t kf = static_cast<size_t>(pl->nterms) * pl->gpad, ka = static_cast<size_t>(pl->nterms) * pl->epad;
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_gbeta, sizeof(float) * ng));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_ebins, sizeof(float) * nbins));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_K, sizeof(double) * nbins * ng));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_B, sizeof(__nv_bfloat16) * nbins * kf));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_BT, sizeof(__nv_bfloat16) * ng * ka));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_A, sizeof(__nv_bfloat16) * max_dist * kf));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_AT, sizeof(__nv_bfloat16) * max_dist * ka));
+  RG_PLAN_CUDA(cudaMalloc(&pl->d_status, sizeof(unsigned)));
+  RG_PLAN_CUDA(cudaMemset(pl->d_status, 0, sizeof(unsigned)));
+  RG_PLAN_CUDA(cudaMemcpy(pl->d_gbeta, gbeta, sizeof(float) * ng, cudaMemcpyHostToDevice));
+  RG_PLAN_CUDA(cudaMemcpy(pl->d_ebins, eb.data(), sizeof(float) * nbins, cudaMemcpyHostToDevice));
+
+  rg::KParams kp {};
+  kp.gbeta      = pl->d_gbeta;
+  kp.ebins      = pl->d_ebins;
+  kp.ng         = ng;
+  kp.nbins      = nbins;
+  kp.log_spaced = pl->log_spaced;
+  kp.ln_k0      = pl->zero ? 0.0 : std::log(K0);
+  kp.mode       = table_mode;
+  if (table_mode == RG_TABLE_REFERENCE) {
+    kp.ln_xmin = ref->ln_xmin;
+    kp.dln     = ref->dln;
+    kp.nseg    = ref->n - 1;
+  } else {
+    kp.ln_xmin = sm->ln_xmin;
+    kp.dln     = sm->dln;
+    kp.nseg    = rg::kSmoothSegments;
+  }
+  kp.ref   = ref->d_coef;
+  kp.hcoef = sm ? sm->d_coef : nullptr;
+  kp.K     = pl->d_K;
+  const int64_t nk = static_cast<int64_t>(nbins) * ng;
+  rg::kernel_matrix_kernel<<<static_cast<unsigned>((nk + 255) / 256), 256>>>(kp);
+  RG_PLAN_CUDA(cudaGetLastError());
+  if (pl->zero) {
+    RG_PLAN_CUDA(cudaMemset(pl->d_K, 0, sizeof(double) * nk));
+  }
+  const int64_t nb = static_cast<int64_t>(nbins) * pl->gpad, nt = static_cast<int64_t>(ng) * pl->epad;
+  rg::split_matrix_kernel<<<static_cast<unsigned>((nb + 255) / 256), 256>>>(pl->d_K, nbins, ng, 0, pl->d_B,
+                                                                            pl->gpad, pl->nterms);
+  RG_PLAN_CUDA(cudaGetLastError());
+  rg::split_matrix_kernel<<<static_cast<unsigned>((nt + 255) / 256), 256>>>(pl->d_K, nbins, ng, 1, pl->d_BT,
+                                                                            pl->epad, pl->nterms);
+  RG_PLAN_CUDA(cudaGetLastError());
+  RG_PLAN_CUDA(cudaDeviceSynchronize());
+  int st = rg::encode_tiled(&pl->tA, pl->d_A, kf, max_dist, rg::kBM);
+  if (st == RG_OK) st = rg::encode_tiled(&pl->tB, pl->d_B, kf, nbins, rg::kBN);
+  if (st == RG_OK) st = rg::encode_tiled(&pl->tAT, pl->d_AT, ka, max_dist, rg::kBM);
+  if (st == RG_OK) st = rg::encode_tiled(&pl->tBT, pl->d_BT, ka, ng, rg::kBN);
+  if (st != RG_OK) {
+    return fail(st);
+  }
+#undef RG_PLAN_CUDA
+  *plan = pl.release();
+  return RG_OK;
+}
+
+int rg_fromdist_plan_destroy(rg_fromdist_plan* pl) {
+  if (!pl) {
+    return RG_OK;
+  }
+  cudaFree(pl->d_gbeta);
+  cudaFree(pl->d_ebins);
+  cudaFree(pl->d_K);
+  cudaFree(pl->d_B);
+  cudaFree(pl->d_BT);
+  cudaFree(pl->d_A);
+  cudaFree(pl->d_AT);
+  cudaFree(pl->d_status);
+  delete pl;
+  return RG_OK;
+}
+
+int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* out, void* stream) {
+  if (!pl || ndist < 0 || ndist > pl->max_dist || (ndist > 0 && (!f || !out))) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_run: bad arguments (ndist above the plan's max_dist?)");
+  }
+  if (ndist == 0) {
+    return RG_OK;
+  }
+  auto          s  = static_cast<cudaStream_t>(stream);
+  const int64_t nA = static_cast<int64_t>(ndist) * pl->gpad;
+  rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
+    f, ndist, pl->ng, pl->ng, nullptr, pl->d_A, pl->gpad, pl->nterms, 0);
+  RG_CUDA_TRY(cudaGetLastError());
+  rg::GemmArgs g {};
+  g.M         = ndist;
+  g.N         = pl->nbins;
+  g.Kp        = pl->nterms * pl->gpad;
+  g.C         = out;
+  g.ldc       = pl->nbins;
+  g.col_scale = pl->d_ebins;
+  g.status    = pl->d_status;
+  return rg::launch_gemm(pl->tA, pl->tB, g, s);
+}
+
+int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndist, float* grad_f, void* stream) {
+  if (!pl || ndist < 0 || ndist > pl->max_dist || (ndist > 0 && (!grad_out || !grad_f))) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_adjoint: bad arguments (ndist above the plan's max_dist?)");
+  }
+  if (ndist == 0) {
+    return RG_OK;
+  }
+  auto          s  = static_cast<cudaStream_t>(stream);
+  const int64_t nA = static_cast<int64_t>(ndist) * pl->epad;
+  // left operand: dL/dS[d][e] * e_e
+  rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
+    grad_out, ndist, pl->nbins, pl->nbins, pl->d_ebins, pl->d_AT, pl->epad, pl->nterms, 0);
+  RG_CUDA_TRY(cudaGetLastError());
+  rg::GemmArgs g {};
+  g.M         = ndist;
+  g.N         = pl->ng;
+  g.Kp        = pl->nterms * pl->epad;
+  g.C         = grad_f;
+  g.ldc       = pl->ng;
+  g.col_scale = nullptr;
+  g.status    = pl->d_status;
+  return rg::launch_gemm(pl->tAT, pl->tBT, g, s);
+}
+
+int rg_fromdist_plan_check(rg_fromdist_plan* pl, void* stream) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  auto     s  = static_cast<cudaStream_t>(stream);
+  unsigned st = 0;
+  RG_CUDA_TRY(cudaMemcpyAsync(&st, pl->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  RG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st != 0) {
+    RG_CUDA_TRY(cudaMemset(pl->d_status, 0, sizeof(unsigned)));
+    return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait in the tensor-core GEMM gave up; results are invalid");
+  }
+  return RG_OK;
+}
+
+int rg_fromdist_kernel_matrix(rg_fromdist_plan* pl, double* K_host) {
+  if (!pl || !K_host) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_kernel_matrix: bad arguments");
+  }
+  RG_CUDA_TRY(cudaMemcpy(K_host, pl->d_K, sizeof(double) * pl->nbins * pl->ng, cudaMemcpyDeviceToHost));
+  return RG_OK;
+}
+
+} // extern "C"

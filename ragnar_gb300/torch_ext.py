@@ -122,3 +122,35 @@ def log_mse(S, S_target, floor: float = 1e-12):
     d = torch.log(torch.where(m, S, torch.ones_like(S))) - torch.log(
         torch.where(m, S_target, torch.ones_like(S_target)))
     return (d * d * m).sum() / m.sum().clamp(min=1)
+
+
+def fromdist_plan(gbeta, bins, g_syn: float = 1.0, e_syn_at_g_syn: float = 1.0, log_spaced: bool = True,
+                  max_dist: int = 1024, smooth: bool = True, split_products: int = 6) -> capi.FromDistPlan:
+    """Tensor-core plan for many distributions on the same gamma bins."""
+    to_np = lambda a: a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)  # noqa: E731
+    mode = capi.RG_TABLE_SMOOTH if smooth else capi.RG_TABLE_REFERENCE
+    return capi.FromDistPlan(to_np(gbeta), log_spaced, to_np(bins), g_syn, e_syn_at_g_syn, max_dist, mode,
+                             split_products)
+
+
+class _FromDistBatched(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan, f):
+        _check(f, "f", f.device)
+        out = torch.empty((f.shape[0], plan.nbins), device=f.device, dtype=torch.float32)
+        plan.run(f, out, _stream(f.device))
+        ctx.plan = plan
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        g = grad_out.contiguous().float()
+        gf = torch.empty((g.shape[0], ctx.plan.ng), device=g.device, dtype=torch.float32)
+        ctx.plan.adjoint(g, gf, _stream(g.device))
+        return None, gf
+
+
+def synchrotron_from_dist_batched(plan: capi.FromDistPlan, f):
+    """Spectra [ndist, nbins] of distributions f [ndist, ng]: BF16 split-precision
+    tensor-core GEMM forward, transpose GEMM adjoint."""
+    return _FromDistBatched.apply(plan, f)
