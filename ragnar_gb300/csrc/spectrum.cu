@@ -103,6 +103,10 @@ namespace rg {
       const uint32_t fmask        = (1u << frac) - 1u;
       const uint32_t hseg         = static_cast<uint32_t>(p.hseg);
       const float    tau_scale    = p.tau_scale;
+      // seg = T >> kFrac as a high multiply by 2^(32 - kFrac) (at most 2^10 whatever
+      // opaque_zero holds, so seg < kRefEntries), fraction bits = T - seg * 2^kFrac
+      const uint32_t seg_mul = (1u << (32 - kFrac)) >> (p.opaque_zero & 31u);
+      const uint32_t seg_neg = (~p.opaque_zero) << kFrac;
 
       int seg_hint = 0;
       if (tid == 0) {
@@ -185,9 +189,10 @@ namespace rg {
           for (int k = 0; k < K; ++k) {
             const uint32_t T = static_cast<uint32_t>(P[k]) - q;
             if (MODE == kModeRef) {
-              const float2 c = tab[T >> kFrac];
-              const float  m = __uint_as_float(T & kFracMask);
-              const float  F = __fmaf_rn(m, c.y, c.x);
+              const uint32_t sg = __umulhi(T, seg_mul);
+              const float2   c  = tab[sg];
+              const float    m  = __uint_as_float(sg * seg_neg + T);
+              const float    F  = __fmaf_rn(m, c.y, c.x);
               acc[k]         = __fmaf_rn(A, F, acc[k]);
             } else {
               const float4 c   = htab[min(T >> frac, hseg)];
@@ -285,34 +290,56 @@ namespace rg {
       double*         acc64; // when set: acc64 += result in FP64 instead of writing out
     };
 
-    __global__ void reduce_partials_kernel(const __grid_constant__ ReduceParams r) {
-      const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    // Block (32 bins x kReduceRows row groups): row group y sums the (block, warp)
+    // partial rows y, y + kReduceRows, ... of its segment, then the row groups are
+    // combined in order through shared memory.  The summation order depends only
+    // on the launch geometry, so results are deterministic.
+    constexpr int kReduceRows = 32;
+
+    __global__ void __launch_bounds__(32 * kReduceRows)
+      reduce_partials_kernel(const __grid_constant__ ReduceParams r) {
+      __shared__ double part[kReduceRows][33];
+      const int bin = blockIdx.x * 32 + threadIdx.x;
       const int s   = blockIdx.y;
-      if (bin >= r.nbins) {
-        return;
-      }
-      double result = 0.0;
-      if (*r.status != kDevOk) {
-        result = __longlong_as_double(0x7ff8000000000000LL);
-      } else {
+      const int ty  = threadIdx.y;
+      const bool failed = *r.status != kDevOk;
+      bool       active = false;
+      double     sum    = 0.0;
+      if (bin < r.nbins && !failed) {
         const int64_t n_items = total_items(r.item_prefix, r.nseg, r.n_single);
         const int64_t i0      = items_before(r.item_prefix, s);
         const int64_t i1      = r.item_prefix ? r.item_prefix[s + 1] : n_items;
         if (i1 > i0 && r.valid[bin]) {
+          active          = true;
           const int b0    = block_of_item(i0, n_items, r.grid);
           const int b1    = block_of_item(i1 - 1, n_items, r.grid);
           const int slice = bin / kSliceBins, j = bin % kSliceBins;
-          double    sum   = 0.0;
-          for (int b = b0; b <= b1; ++b) {
-            const double* base =
-              r.partials + (static_cast<int64_t>(b + s) * r.nslices + slice) * kWarps * kSliceBins + j;
-#pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-              sum += base[w * kSliceBins];
-            }
+          const int rows  = (b1 - b0 + 1) * kWarps;
+          const double* base =
+            r.partials + (static_cast<int64_t>(b0 + s) * r.nslices + slice) * kWarps * kSliceBins + j;
+          const int64_t block_stride = static_cast<int64_t>(r.nslices) * kWarps * kSliceBins;
+#pragma unroll 4
+          for (int row = ty; row < rows; row += kReduceRows) {
+            const int bb = row / kWarps, w = row % kWarps;
+            sum += base[bb * block_stride + w * kSliceBins];
           }
-          result = sum * static_cast<double>(r.ebins[bin]);
         }
+      }
+      part[ty][threadIdx.x] = sum;
+      __syncthreads();
+      if (ty != 0 || bin >= r.nbins) {
+        return;
+      }
+      double result = 0.0;
+      if (failed) {
+        result = __longlong_as_double(0x7ff8000000000000LL);
+      } else if (active) {
+        double t = 0.0;
+#pragma unroll
+        for (int y = 0; y < kReduceRows; ++y) {
+          t += part[y][threadIdx.x];
+        }
+        result = t * static_cast<double>(r.ebins[bin]);
       }
       const int64_t o = static_cast<int64_t>(s) * r.nbins + bin;
       if (r.acc64) {
@@ -715,7 +742,7 @@ namespace rg {
     rp.status      = status;
     rp.out         = out;
     rp.acc64       = nullptr;
-    reduce_partials_kernel<<<dim3((nbins + 127) / 128, 1), 128, 0, s>>>(rp);
+    reduce_partials_kernel<<<dim3((nbins + 31) / 32, 1), dim3(32, kReduceRows), 0, s>>>(rp);
     RG_CUDA_TRY(cudaGetLastError());
     return RG_OK;
   }
@@ -773,8 +800,8 @@ namespace rg {
       rp.status      = pl->d_status;
       rp.out         = out;
       rp.acc64       = acc64;
-      dim3 rgrid((pl->nbins + 127) / 128, nseg);
-      reduce_partials_kernel<<<rgrid, 128, 0, s>>>(rp);
+      dim3 rgrid((pl->nbins + 31) / 32, nseg);
+      reduce_partials_kernel<<<rgrid, dim3(32, kReduceRows), 0, s>>>(rp);
       RG_CUDA_TRY(cudaGetLastError());
       return RG_OK;
     }

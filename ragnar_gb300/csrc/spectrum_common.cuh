@@ -56,6 +56,11 @@ namespace rg {
     double*        partials;     // [(grid + nseg) * nslices * kWarps * kSliceBins]
     int            nslices;
     unsigned*      status;
+    // Always 0 (zero-initialised with the struct).  The kernel builds its integer
+    // multipliers from it, so the compiler cannot fold them into shifts and masks:
+    // the per-eval coordinate arithmetic then runs as IMAD on the FMA pipe instead
+    // of on the half-rate integer ALU pipe.
+    uint32_t       opaque_zero;
   };
 
   struct ItemInfo {
