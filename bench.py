@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--profile-case", action="store_true",
@@ -394,6 +396,8 @@ def run_ours(args, rank, world, local_rank):
     }
 
     extra = {"spectra_finite": spectra_ok}
+    if rank == 0 and not args.no_extras:
+        extra["energy_distribution_dump"] = guarded(histogram_case, torch, capi, device, comps, NSPECIES * n_per)
     # e2e: host-resident pinned inputs through the C ABI, copies inside the timed region
     if not args.no_e2e:
         host = [torch.empty(c.numel(), dtype=torch.float32, pin_memory=True) for c in comps]
@@ -439,8 +443,14 @@ def run_ours(args, rank, world, local_rank):
 
     # context beside the headline: the plain one-spectrum-per-launch kernel on one
     # species, and the 1e6-particle x 200-bin configuration (fused and plain)
-    if rank == 0:
-        extra.update(side_measurements(torch, capi, device, stream))
+    if rank == 0 and not args.no_extras:
+        extra.update(guarded(side_measurements, torch, capi, device, stream))
+        extra["batched_graph_256_segments"] = guarded(batched_graph_case, torch, capi, device)
+        extra["fwd_adjoint_1e7x512"] = guarded(fwd_adjoint_case, torch, capi, device)
+        peak_bf16, peak_src = measured_peak("bf16_tflops", 1900.0)
+        extra["fromdist_gemm_4096x1024x1024"] = guarded(fromdist_gemm_case, torch, capi, device, peak_bf16)
+        extra["fromdist_gemm_4096x1024x1024"]["peak_source"] = peak_src
+        extra["adam_fit_1024x512x512"] = guarded(adam_fit_case, torch, capi, device)
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     result["extra"] = extra
@@ -450,51 +460,297 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(result), flush=True)
 
 
-def side_measurements(torch, capi, device, stream):
+def guarded(fn, *a):
+    """Runs one side case; a failure is reported in the JSON line instead of ending the run."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def measured_peak(key, fallback):
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)[key]), "measured"
+    except (OSError, KeyError, ValueError):
+        return fallback, "fallback"
+
+
+def timed(torch, fn, reps, warm=2):
+    """Seconds per call of fn, CUDA events on the current stream after `warm` calls."""
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3 / reps
+
+
+def logbins(capi, lo, hi, n):
     import numpy as np  # noqa: PLC0415
 
+    b = np.empty(n, np.float32)
+    capi.check(capi.lib().rg_logspace(lo, hi, n, b.ctypes.data))
+    return b
+
+
+def config1_particles(torch, n, gen, device, index=-2.0):
+    """|u| ~ |u|^index on [1, 100] (per-particle index allowed), isotropic, B = z."""
+    q = index + 1.0
+    r = torch.rand(n, device=device, generator=gen, dtype=torch.float64)
+    umag = ((100.0**q - 1.0) * r + 1.0) ** (1.0 / q)
+    return isotropic_torch(torch, umag.float(), gen)
+
+
+def side_measurements(torch, capi, device, stream):
+    """The plain one-spectrum-per-launch kernel beside the fused one, and the
+    1e6-particle x 200-bin configuration."""
     out = {}
-
-    def timed(fn, reps):
-        fn()
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(reps):
-            fn()
-        b.record()
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3 / reps
-
     n = 8_000_000
     comps = make_particles(torch, n, 1, device, seed=77)
     prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
-    bins = photon_bins()
-    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    plan = capi.SpectrumPlan(photon_bins(), 1.0, 1.0, 1.0)
     o = torch.empty(NBINS, device=device)
-    t_f = timed(lambda: plan.run(prt, o, stream), 10)
-    t_p = timed(lambda: plan.run_plain(prt, o, stream), 2)
-    out["dump_species_8e6_fused_evals_per_s"] = n * NBINS / t_f
-    out["dump_species_8e6_plain_evals_per_s"] = n * NBINS / t_p
+    out["dump_species_8e6_fused_evals_per_s"] = n * NBINS / timed(torch, lambda: plan.run(prt, o, stream), 10)
+    out["dump_species_8e6_plain_evals_per_s"] = n * NBINS / timed(torch, lambda: plan.run_plain(prt, o, stream), 2)
     plan.close()
-    # configuration 1: 1e6 particles, |u| ~ u^-2 on [1,100], B = z, 200 bins 0.01..1e7
+    del comps
     n1 = 1_000_000
     gen = torch.Generator(device=device).manual_seed(5)
-    umag = 1.0 / (1.0 - torch.rand(n1, device=device, generator=gen) * (1 - 1e-2))
-    u1 = isotropic_torch(torch, umag, gen)
+    u1 = config1_particles(torch, n1, gen, device)
     z = torch.zeros(n1, device=device)
     prt1 = capi.particles(u1, b=[z, z, torch.ones(n1, device=device)], n=n1)
-    b1 = np.empty(200, np.float32)
-    capi.check(capi.lib().rg_logspace(0.01, 1e7, 200, b1.ctypes.data))
-    plan1 = capi.SpectrumPlan(b1, 1.0, 1.0, 1.0)
+    plan1 = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 200), 1.0, 1.0, 1.0)
     o1 = torch.empty(200, device=device)
-    t1f = timed(lambda: plan1.run(prt1, o1, stream), 20)
-    t1p = timed(lambda: plan1.run_plain(prt1, o1, stream), 5)
-    out["config1_fused_evals_per_s"] = n1 * 200 / t1f
-    out["config1_plain_evals_per_s"] = n1 * 200 / t1p
+    out["config1_fused_evals_per_s"] = n1 * 200 / timed(torch, lambda: plan1.run(prt1, o1, stream), 20)
+    out["config1_plain_evals_per_s"] = n1 * 200 / timed(torch, lambda: plan1.run_plain(prt1, o1, stream), 5)
     plan1.close()
     return out
+
+
+def batched_graph_case(torch, capi, device):
+    """256 spectra of uneven size (counts log-uniform on [1e4, 1e7], power-law index
+    uniform on [-3, -1.5] per segment, 200 bins 0.01..1e7): one persistent launch
+    replayed from a CUDA graph, against the same launch eagerly and against one
+    launch per segment."""
+    nseg, nb = 256, 200
+    gen = torch.Generator(device=device).manual_seed(303)
+    counts = torch.floor(10.0 ** (4.0 + 3.0 * torch.rand(nseg, device=device, generator=gen,
+                                                           dtype=torch.float64))).long()
+    total = int(counts.sum())
+    offs = torch.zeros(nseg + 1, dtype=torch.int64, device=device)
+    offs[1:] = torch.cumsum(counts, 0)
+    index = -3.0 + 1.5 * torch.rand(nseg, device=device, generator=gen, dtype=torch.float64)
+    u = config1_particles(torch, total, gen, device,
+                          index=torch.repeat_interleave(index, counts))
+    bz = torch.ones(total, device=device)
+    prt = capi.particles(u, b=[None, None, bz], n=total)
+    plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, nb), 1.0, 1.0, 1.0)
+    plan.reserve(nseg)
+    out = torch.empty((nseg, nb), device=device)
+    side = torch.cuda.Stream(device)
+    side.wait_stream(torch.cuda.current_stream(device))
+    with torch.cuda.stream(side):
+        plan.run_batched(prt, offs, nseg, out, side.cuda_stream)
+    torch.cuda.current_stream(device).wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.run_batched(prt, offs, nseg, out, torch.cuda.current_stream(device).cuda_stream)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    t_graph = timed(torch, graph.replay, 10)
+    ref = out.clone()
+    t_eager = timed(torch, lambda: plan.run_batched(prt, offs, nseg, out, stream), 10)
+    same = bool(torch.equal(out, ref))
+    host_offs = offs.cpu().tolist()
+    segs = [capi.particles([c[a:b] for c in u], b=[None, None, bz[a:b]], n=b - a)
+            for a, b in zip(host_offs[:-1], host_offs[1:])]
+
+    def per_segment():
+        for s in range(nseg):
+            plan.run(segs[s], out[s], stream)
+
+    t_loop = timed(torch, per_segment, 3, warm=1)
+    plan.check(stream)
+    plan.close()
+    evals = total * nb
+    return {"segments": nseg, "particles": total, "photon_bins": nb,
+            "graph_evals_per_s": evals / t_graph, "graph_ms": t_graph * 1e3,
+            "eager_batched_evals_per_s": evals / t_eager,
+            "one_launch_per_segment_evals_per_s": evals / t_loop,
+            "graph_equals_eager": same}
+
+
+def fwd_adjoint_case(torch, capi, device):
+    """1e7 particles (|u| ~ u^-2 on [1, 100], isotropic, B = z, w = 1) x 512 bins
+    0.01..1e7 with the smooth (differentiable) table: forward, adjoint, and the
+    plain reference-table kernel on the same particles."""
+    n, nb = 10_000_000, 512
+    gen = torch.Generator(device=device).manual_seed(404)
+    u = config1_particles(torch, n, gen, device)
+    z = torch.zeros(n, device=device)
+    w = torch.ones(n, device=device)
+    prt = capi.particles(u, b=[z, z, torch.ones(n, device=device)], w=w, n=n)
+    bins = logbins(capi, 0.01, 1e7, nb)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
+    S = torch.empty(nb, device=device)
+    gS = torch.rand(nb, device=device, generator=gen)
+    gw = torch.empty(n, device=device)
+    gu = [torch.empty(n, device=device) for _ in range(3)]
+    stream = torch.cuda.current_stream(device).cuda_stream
+    t_fwd = timed(torch, lambda: plan.run(prt, S, stream), 10)
+    t_adj = timed(torch, lambda: plan.adjoint(prt, gS, gw, gu, stream), 10)
+
+    def step():
+        plan.run(prt, S, stream)
+        plan.adjoint(prt, gS, gw, gu, stream)
+
+    t_step = timed(torch, step, 10)
+    plan.check(stream)
+    plain = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    t_plain = timed(torch, lambda: plain.run_plain(prt, S, stream), 3)
+    plain.close()
+    plan.close()
+    evals = n * nb
+    return {"particles": n, "photon_bins": nb, "table": "smooth",
+            "fwd_evals_per_s": evals / t_fwd, "adjoint_evals_per_s": evals / t_adj,
+            "fwd_plus_adjoint_evals_per_s": evals / t_step, "fwd_plus_adjoint_ms": t_step * 1e3,
+            "plain_fwd_evals_per_s": evals / t_plain}
+
+
+def fromdist_gemm_case(torch, capi, device, peak_bf16):
+    """4096 distributions on 1024 log gamma bins [1, 1e6] (power laws, index uniform
+    on [-3, -1.5], random cutoffs) -> 1024 photon bins 1e-2..1e13 through the
+    split-precision tcgen05 GEMM; error against the FP64 product of the plan's
+    own FP64 kernel matrix."""
+    import numpy as np  # noqa: PLC0415
+
+    nd, ng, ne = 4096, 1024, 1024
+    gb = logbins(capi, 1.0, 1e6, ng)
+    bins = logbins(capi, 1e-2, 1e13, ne)
+    rng = np.random.default_rng(505)
+    g = gb.astype(np.float64)[None, :]
+    p = rng.uniform(-3.0, -1.5, (nd, 1))
+    lo = 10.0 ** rng.uniform(0.0, 2.0, (nd, 1))
+    hi = 10.0 ** rng.uniform(3.0, 6.0, (nd, 1))
+    f_np = np.where((g >= lo) & (g < hi), g**p, 0.0).astype(np.float32)
+    f = torch.from_numpy(f_np).to(device)
+    out = torch.empty((nd, ne), device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    res = {"distributions": nd, "gamma_bins": ng, "photon_bins": ne}
+    for terms in (6, 3):
+        plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=nd, split_products=terms)
+        t = timed(torch, lambda: plan.run(f, out, stream), 20)
+        plan.check(stream)
+        K = plan.kernel_matrix()
+        S = out.cpu().numpy().astype(np.float64)
+        S64 = (f_np.astype(np.float64) @ K.T) * bins.astype(np.float64)[None, :]
+        m = S64 > 1e-12 * S64.max(axis=1, keepdims=True)
+        err = float(np.max(np.abs(S[m] - S64[m]) / S64[m]))
+        flops = 2.0 * nd * ng * ne * terms
+        res[f"bf16x{terms}"] = {
+            "evals_per_s": nd * ng * ne / t, "ms": t * 1e3, "bf16_tflops": flops / t / 1e12,
+            "frac_of_bf16_peak": flops / t / 1e12 / peak_bf16, "max_rel_err_vs_fp64": err}
+        plan.close()
+    res["peak_bf16_tflops"] = peak_bf16
+    return res
+
+
+def adam_fit_case(torch, capi, device, steps=200):
+    """1024 distributions of 512 log gamma bins [1, 1e5] fitted by Adam to target
+    spectra of random broken power laws (indices uniform on [-3.5, -1.2], break
+    log-uniform on [10, 1e4]) on 512 photon bins 1e-2..1e11; loss = log-space MSE.
+    Gradients w.r.t. the distribution values flow through the GEMM forward and its
+    transpose-GEMM adjoint; errors of the final forward and gradient are against
+    FP64 products of the plan's FP64 kernel matrix."""
+    import numpy as np  # noqa: PLC0415
+
+    from ragnar_gb300 import torch_ext as rt  # noqa: PLC0415
+
+    nd, ng, ne = 1024, 512, 512
+    gb = logbins(capi, 1.0, 1e5, ng)
+    bins = logbins(capi, 1e-2, 1e11, ne)
+    plan = rt.fromdist_plan(gb, bins, max_dist=nd)
+    gen = torch.Generator(device=device).manual_seed(606)
+    lg = torch.log(torch.from_numpy(gb).to(device).double())[None, :]
+    p1 = -3.5 + 2.3 * torch.rand((nd, 1), device=device, generator=gen, dtype=torch.float64)
+    p2 = -3.5 + 2.3 * torch.rand((nd, 1), device=device, generator=gen, dtype=torch.float64)
+    lb = math.log(10.0) * (1.0 + 3.0 * torch.rand((nd, 1), device=device, generator=gen, dtype=torch.float64))
+    f_t = torch.exp(torch.where(lg < lb, p1 * lg, p1 * lb + p2 * (lg - lb))).float()
+    with torch.no_grad():
+        S_t = rt.synchrotron_from_dist_batched(plan, f_t)
+    m_t = S_t > 1e-12 * S_t.amax(dim=1, keepdim=True)
+    theta = (-2.0 * lg).float().repeat(nd, 1).contiguous().requires_grad_(True)
+    opt = torch.optim.Adam([theta], lr=0.05)
+
+    def loss_of(S):
+        m = m_t & (S > 1e-12 * S.detach().amax(dim=1, keepdim=True))
+        d = torch.log(torch.where(m, S, torch.ones_like(S))) - torch.log(torch.where(m, S_t, torch.ones_like(S)))
+        return (d * d * m).sum() / m.sum().clamp(min=1)
+
+    def step():
+        opt.zero_grad(set_to_none=True)
+        loss = loss_of(rt.synchrotron_from_dist_batched(plan, torch.exp(theta)))
+        loss.backward()
+        opt.step()
+        return loss
+
+    l0 = float(step().detach())
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps - 1):
+        loss = step()
+    b.record()
+    torch.cuda.synchronize()
+    t_step = a.elapsed_time(b) / 1e3 / (steps - 1)
+    l1 = float(loss.detach())
+    # final forward and gradient against FP64
+    f = torch.exp(theta.detach()).contiguous().requires_grad_(True)
+    S = rt.synchrotron_from_dist_batched(plan, f)
+    loss = loss_of(S)
+    gS, = torch.autograd.grad(loss, S, retain_graph=True)
+    loss.backward()
+    K = plan.kernel_matrix()
+    e = bins.astype(np.float64)[None, :]
+    f64 = f.detach().cpu().numpy().astype(np.float64)
+    S64 = (f64 @ K.T) * e
+    Sg = S.detach().cpu().numpy()
+    mm = S64 > 1e-12 * S64.max(axis=1, keepdims=True)
+    g64 = (gS.cpu().numpy().astype(np.float64) * e) @ K
+    gg = f.grad.cpu().numpy()
+    plan.check()
+    plan.close()
+    return {"distributions": nd, "gamma_bins": ng, "photon_bins": ne, "adam_steps": steps,
+            "ms_per_adam_step": t_step * 1e3, "gemm_evals_per_s": 2.0 * nd * ng * ne / t_step,
+            "loss_first": l0, "loss_last": l1,
+            "fwd_max_rel_err_vs_fp64": float(np.max(np.abs(Sg[mm] - S64[mm]) / S64[mm])),
+            "grad_max_err_vs_fp64_rel_to_row_max": float(np.max(np.abs(gg - g64) /
+                                                                np.max(np.abs(g64), axis=1, keepdims=True)))}
+
+
+def histogram_case(torch, capi, device, comps, n):
+    """Particles.energyDistribution of the dump-scale particles into 200 log gamma-beta
+    bins 1e-2..1e3 (12 B/particle read: the HBM-bound kernel)."""
+    import numpy as np  # noqa: PLC0415
+
+    bins = logbins(capi, 1e-2, 1e3, 200)
+    hist = torch.empty(200, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+
+    def run():
+        capi.check(capi.lib().rg_energy_distribution(comps[0].data_ptr(), comps[1].data_ptr(),
+                                                     comps[2].data_ptr(), n, bins.ctypes.data, 200, 1, 1,
+                                                     hist.data_ptr(), None, stream))
+
+    t = timed(torch, run, 10)
+    return {"particles": n, "bins": 200, "particles_per_s": n / t, "ms": t * 1e3,
+            "hbm_gbs": 12.0 * n / t / 1e9}
 
 
 def profile_case():

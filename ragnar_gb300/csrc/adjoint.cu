@@ -114,7 +114,17 @@ namespace rg {
       const int64_t n_items  = total_items(p.item_prefix, p.nseg, p.n_single);
       const int64_t it_begin = static_cast<int64_t>(b) * n_items / G;
       const int64_t it_end   = static_cast<int64_t>(b + 1) * n_items / G;
-      if (it_begin >= it_end || *p.status != kDevOk) {
+      if (it_begin >= it_end) {
+        return;
+      }
+      if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+      }
+      // one block-wide decision on the status word, and the barriers are
+      // initialised before any thread waits on them
+      if (__syncthreads_or(*p.status != kDevOk)) {
         return;
       }
       if (MODE == kModeRef) {
@@ -141,9 +151,6 @@ namespace rg {
 
       int seg_hint = 0;
       if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-        fence_mbar_init();
         info[0] = item_info(p, it_begin, seg_hint);
         if (p.use_tma) {
           issue_stage(p, info[0], stage, &mbar[0]);

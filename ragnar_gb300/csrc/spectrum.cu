@@ -79,7 +79,17 @@ namespace rg {
       const int64_t n_items  = total_items(p.item_prefix, p.nseg, p.n_single);
       const int64_t it_begin = static_cast<int64_t>(b) * n_items / G;
       const int64_t it_end   = static_cast<int64_t>(b + 1) * n_items / G;
-      if (it_begin >= it_end || *p.status != kDevOk) {
+      if (it_begin >= it_end) {
+        return;
+      }
+      if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+      }
+      // one block-wide decision on the status word, and the barriers are
+      // initialised before any thread waits on them
+      if (__syncthreads_or(*p.status != kDevOk)) {
         return;
       }
       if (MODE == kModeRef) {
@@ -110,9 +120,6 @@ namespace rg {
 
       int seg_hint = 0;
       if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-        fence_mbar_init();
         info[0] = item_info(p, it_begin, seg_hint);
         if (p.use_tma) {
           issue_stage(p, info[0], stage, &mbar[0]);
@@ -321,7 +328,11 @@ namespace rg {
 #pragma unroll 4
           for (int row = ty; row < rows; row += kReduceRows) {
             const int bb = row / kWarps, w = row % kWarps;
-            sum += base[bb * block_stride + w * kSliceBins];
+            // a block that owns no item (more blocks than items) wrote no partials
+            const int64_t b = b0 + bb;
+            if (b * n_items / r.grid < (b + 1) * n_items / r.grid) {
+              sum += base[bb * block_stride + w * kSliceBins];
+            }
           }
         }
       }
@@ -919,6 +930,10 @@ int rg_spectrum_plan_check(rg_spectrum_plan* pl, void* stream) {
     if (st & rg::kDevBadOffsets) {
       return rg::set_error(RG_ERR_ARGUMENT,
                            "segment offsets must be non-decreasing, >= 0 and <= the particle count");
+    }
+    if (st & rg::kDevBadIndex) {
+      return rg::set_error(RG_ERR_CUDA, "a particle-stream index self-check failed on the GPU (status " +
+                                          std::to_string(st) + "); results are invalid");
     }
     return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait on the GPU gave up (status " + std::to_string(st) +
                                            "); results are invalid");

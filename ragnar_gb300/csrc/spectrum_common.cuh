@@ -23,6 +23,7 @@ namespace rg {
 
   // extra status bit: segment offsets were not non-decreasing / within [0, n]
   constexpr unsigned kDevBadOffsets = 4u;
+  constexpr unsigned kDevBadIndex   = 8u; // a staging self-check found an out-of-range span; access skipped
 
   enum Source : int { kSrcParticles = 0, kSrcDist = 1 };
   enum Mode : int { kModeRef = RG_TABLE_REFERENCE, kModeSmooth = RG_TABLE_SMOOTH };
@@ -233,7 +234,18 @@ namespace rg {
   // [a0, a1) of every staged stream into `buf`, completing on `bar`.
   __device__ __forceinline__ void issue_stage(const FusedParams& p, const ItemInfo& I, float* buf,
                                               uint64_t* bar) {
-    const uint32_t bytes = static_cast<uint32_t>(I.a1 - I.a0) * 4u;
+    // self-check: the span lies inside the streams (n_single is the stream length),
+    // fits the staging slot, and every source address is 16-byte aligned
+    bool ok = I.a0 >= 0 && I.a0 <= I.a1 && I.a1 <= p.n_single && I.a1 - I.a0 <= kChunkPad;
+    for (int c = 0; c < kComps && ok; ++c) {
+      if (p.slot[c] >= 0) {
+        ok = (reinterpret_cast<uintptr_t>(p.comp[c] + I.a0) & 15u) == 0;
+      }
+    }
+    if (!ok) {
+      atomicOr(p.status, kDevBadIndex);
+    }
+    const uint32_t bytes = ok ? static_cast<uint32_t>(I.a1 - I.a0) * 4u : 0u;
     mbar_arrive_expect_tx(bar, bytes * static_cast<uint32_t>(p.nslots));
     if (bytes) {
       for (int c = 0; c < kComps; ++c) {
@@ -248,12 +260,21 @@ namespace rg {
   __device__ __forceinline__ void load_comps(const FusedParams& p, const ItemInfo& I,
                                              const float* sbuf, int64_t gp, float (&v)[kComps]) {
     const bool in_smem = p.use_tma && gp < I.a1;
+    // self-check of the direct loads: gp inside the streams
+    const bool in_range = gp >= 0 && gp < p.n_single;
+    if (!in_smem && !in_range) {
+      atomicOr(p.status, kDevBadIndex);
+    }
 #pragma unroll
     for (int c = 0; c < kComps; ++c) {
       const float* src = p.comp[c];
       v[c]             = 0.0f;
       if (src) {
-        v[c] = in_smem ? sbuf[p.slot[c] * kChunkPad + (gp - I.a0)] : __ldg(src + gp);
+        if (in_smem) {
+          v[c] = sbuf[p.slot[c] * kChunkPad + (gp - I.a0)];
+        } else if (in_range) {
+          v[c] = __ldg(src + gp);
+        }
       }
     }
   }

@@ -166,6 +166,43 @@ def test_batched_segments(gpu, oracle_lib, table):
             assert max_rel(got[s], truth[s]) <= SPECTRUM_RTOL, s
 
 
+def test_batched_run_replays_from_cuda_graph(gpu, oracle_lib, table):
+    """The batched launch captured once into a CUDA graph: each replay reads the
+    particle streams and offsets as they are at replay time."""
+    P = particles(50000, seed=12, bfield="iso", weights=True)
+    bins = oracle_lib.logspace(0.01, 1e7, 300)
+    T, prt = to_device(P, gpu)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    plan.reserve(4)
+    offs = torch.tensor([0, 7000, 7000, 31000, 50000], dtype=torch.int64, device=gpu)
+    out = torch.empty((4, 300), device=gpu)
+    side = torch.cuda.Stream(gpu)
+    side.wait_stream(torch.cuda.current_stream(gpu))
+    with torch.cuda.stream(side):
+        plan.run_batched(prt, offs, 4, out, side.cuda_stream)
+    torch.cuda.current_stream(gpu).wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.run_batched(prt, offs, 4, out, torch.cuda.current_stream(gpu).cuda_stream)
+    for scale, cuts in ((1.0, [0, 7000, 7000, 31000, 50000]), (0.5, [0, 100, 25000, 25001, 50000])):
+        T["w"].copy_(torch.from_numpy(P["w"] * np.float32(scale)))
+        offs.copy_(torch.tensor(cuts, dtype=torch.int64))
+        graph.replay()
+        plan.check()
+        eager = torch.empty_like(out)
+        plan.run_batched(prt, offs, 4, eager)
+        plan.check()
+        assert torch.equal(out, eager)
+        Pw = dict(P, w=P["w"] * np.float32(scale))
+        truth = oracle_lib.sync_spectrum_batched_f64(Pw, np.array(cuts, np.int64), bins, 1.0, 1.0, 1.0, table)
+        got = out.cpu().numpy()
+        for s in range(4):
+            if cuts[s + 1] == cuts[s]:
+                assert np.all(got[s] == 0)
+            else:
+                assert max_rel(got[s], truth[s]) <= SPECTRUM_RTOL, (scale, s)
+
+
 def test_batched_rejects_bad_offsets(gpu, oracle_lib):
     P = particles(1000, seed=1)
     T, prt = to_device(P, gpu)
