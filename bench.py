@@ -308,7 +308,7 @@ def run_ours(args, rank, world, local_rank):
     import numpy as np  # noqa: PLC0415
     import torch  # noqa: PLC0415
 
-    from ragnar_gb300 import capi  # noqa: PLC0415
+    from ragnar_gb300 import capi, shard  # noqa: PLC0415
 
     dist = world > 1
     device = torch.device("cuda", local_rank)
@@ -367,9 +367,7 @@ def run_ours(args, rank, world, local_rank):
     plan_p.check(stream)
     spectra_ok = bool(torch.isfinite(out_e).all() and torch.isfinite(out_p).all() and out_e.sum() > 0)
     if dist:
-        t = torch.tensor([t_step], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
+        t_step = shard.max_over_ranks(t_step, device)
 
     # fused-kernel roofline: FP32-core issue slots (SMs x 128 lanes x clock)
     kern_ms = (ke_ms + kp_ms) / max(ke_n + kp_n, 1)
@@ -429,9 +427,7 @@ def run_ours(args, rank, world, local_rank):
             e2e_step()
         t_e2e = (time.perf_counter() - t0) / max(args.steps, 1)
         if dist:
-            t = torch.tensor([t_e2e], device=device)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            t_e2e = float(t.item())
+            t_e2e = shard.max_over_ranks(t_e2e, device)
         result["e2e"] = {"value": world * evals_per_step / t_e2e, "unit": UNIT,
                          "h2d_bytes_per_step": 7 * 4 * NSPECIES * n_per,
                          "d2h_bytes_per_step": 4 * NSPECIES * NBINS,
