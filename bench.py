@@ -57,9 +57,10 @@ def parse_args():
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="small case for ncu captures: one 4.19e6-particle species x 512 bins, "
-                         "4 fused-kernel launches, then exit")
+    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm"],
+                    help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
+                         "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
+                         "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches")
     return ap.parse_args()
 
 
@@ -773,10 +774,36 @@ def profile_case():
     print("profile case done")
 
 
+def profile_gemm_case():
+    """4 launches of the split + tcgen05 GEMM forward on 4096 x 1024 x 1024 (6 products)."""
+    import numpy as np  # noqa: PLC0415
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    gb = logbins(capi, 1.0, 1e6, 1024)
+    bins = logbins(capi, 1e-2, 1e13, 1024)
+    rng = np.random.default_rng(505)
+    f = torch.from_numpy((gb.astype(np.float64)[None, :] ** rng.uniform(-3.0, -1.5, (4096, 1)))
+                         .astype(np.float32)).to(device)
+    out = torch.empty((4096, 1024), device=device)
+    plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=4096)
+    for _ in range(4):
+        plan.run(f, out, torch.cuda.current_stream().cuda_stream)
+    plan.check()
+    plan.close()
+    print("profile gemm case done")
+
+
 def main():
     args = parse_args()
-    if args.profile_case:
+    if args.profile_case == "spectrum":
         profile_case()
+        return
+    if args.profile_case == "gemm":
+        profile_gemm_case()
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -132,9 +132,7 @@ namespace rg {
           tab[i] = p.table[i];
         }
       } else {
-        for (int i = tid; i <= p.hseg; i += kThreads) {
-          htab[i] = p.htable[i];
-        }
+        stage_smooth_table(p, htab, tid, kThreads);
       }
       int32_t P[K];
 #pragma unroll
@@ -145,9 +143,9 @@ namespace rg {
       const int      stage_floats = p.nslots * kChunkPad;
       const uint32_t dead         = dead_coordinate(Pmin, p.L);
       const int      frac         = (MODE == kModeRef) ? kFrac : p.frac;
-      const uint32_t fmask        = (1u << frac) - 1u;
       const uint32_t hseg         = static_cast<uint32_t>(p.hseg);
-      const float    tau_scale    = p.tau_scale;
+      // fraction bits = T - seg * 2^frac as an IMAD, opaque to the compiler
+      const uint32_t seg_neg      = (~p.opaque_zero) << frac;
 
       int seg_hint = 0;
       if (tid == 0) {
@@ -220,14 +218,15 @@ namespace rg {
 #pragma unroll
               for (int k = 0; k < K; ++k) {
                 const uint32_t T = static_cast<uint32_t>(P[k]) - q;
+                const uint32_t sg = T >> frac;
                 if (MODE == kModeRef) {
-                  const float2 c = tab[T >> kFrac];
-                  const float  m = __uint_as_float(T & kFracMask);
+                  const float2 c = tab[sg];
+                  const float  m = __uint_as_float(sg * seg_neg + T);
                   r1             = __fmaf_rn(Gk[k], __fmaf_rn(m, c.y, c.x), r1);
                   r2             = __fmaf_rn(Gk[k], c.y, r2);
                 } else {
-                  const float4 c   = htab[min(T >> frac, hseg)];
-                  const float  tau = __uint2float_rn(T & fmask) * tau_scale;
+                  const float4 c   = htab[min(sg, hseg)];
+                  const float  tau = smooth_tau(sg * seg_neg + T);
                   const float  p2  = __fmaf_rn(tau, c.w, c.z);
                   const float  F   = __fmaf_rn(tau, __fmaf_rn(tau, p2, c.y), c.x);
                   const float  dF  = __fmaf_rn(tau, __fmaf_rn(tau, c.w, p2 + p2), c.y);
@@ -357,7 +356,9 @@ namespace rg {
       x.ebins    = pl->d_ebins;
       x.valid    = pl->d_valid;
       x.nbins    = pl->nbins;
-      x.dscale   = static_cast<float>((pl->table_mode == kModeRef ? 1.0 / kSlopeScale : 1.0) / dln);
+      // reference slopes carry 2^127; smooth slopes are per tau' = tau 2^(frac - 23)
+      x.dscale   = static_cast<float>((pl->table_mode == kModeRef ? 1.0 / kSlopeScale
+                                                                  : std::ldexp(1.0, pl->frac - 23)) / dln);
       x.gw       = gw;
       for (int d = 0; d < 3; ++d) {
         x.gu[d] = gu[d];

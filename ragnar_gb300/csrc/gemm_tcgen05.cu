@@ -9,16 +9,21 @@
 // Precision: FP32 operands are split into BF16 terms (x = h + m + l, each the
 // BF16 rounding of the remainder) and the products are summed in one GEMM over
 // a concatenated K dimension, accumulated in FP32 in tensor memory:
-//   6 products  (h.h + h.m + m.h + h.l + l.h + m.m): ~1e-8 relative (default)
-//   3 products  (h.h + h.m + m.h):                  ~1e-5 relative (fast)
+//   6 products  (h.h + h.m + m.h + h.l + l.h + m.m): ~1e-8 relative per product (default)
+//   3 products  (h.h + h.m + m.h):                  ~1e-5 relative per product (fast)
+// The dominant h.h product accumulates in its own TMEM accumulator and the
+// correction products in a second one; the epilogue adds the two.  The FP32
+// accumulator is rounded once per MMA, so keeping the small corrections out of
+// the large running sum bounds the accumulation error by the h.h steps alone
+// (4 per 64 gamma bins) instead of by all of them.
 //
 // GEMM: C[M x N] = A[M x K'] . B[N x K']^T, both operands K-major BF16.  CTA tile
 // 128 x 256, K step 64; TMA (cp.async.bulk.tensor, 128-byte swizzle) fills a
 // 4-stage shared-memory ring; one thread issues tcgen05.mma (M 128, N 256, K 16)
-// into a 128 x 256 FP32 accumulator in tensor memory and commits each stage
-// back to the producer; after the last commit all four warps read the
-// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
-// C * col_scale.  Every mbarrier wait is bounded; a wait that gives up records
+// into one of two 128 x 256 FP32 accumulators in tensor memory and commits
+// each stage back to the producer; after the last commit all four warps read
+// both accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and
+// write (acc0 + acc1) * col_scale.  Every mbarrier wait is bounded; a wait that gives up records
 // the status word, and the CTA still frees its tensor memory.
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
@@ -45,7 +50,7 @@ namespace rg {
     constexpr int kGemmThreads = 128;
     constexpr uint32_t kBytesA = kBM * kBK * 2;
     constexpr uint32_t kBytesB = kBN * kBK * 2;
-    constexpr uint32_t kTmemCols = 256;
+    constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
     constexpr unsigned kDevGemmTimeout = 8u;
 
     __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y,
@@ -119,6 +124,7 @@ namespace rg {
 
     struct GemmArgs {
       int          M, N, Kp; // Kp: concatenated K, a multiple of kBK
+      int          kb_lead;  // k blocks of the leading (h.h) product: accumulator 0
       float*       C;
       int          ldc;
       const float* col_scale; // nullable
@@ -178,6 +184,7 @@ namespace rg {
       } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----------------------------------------------------------------
         bool ok = true;
+        uint32_t started = 0; // bit a: accumulator a holds a partial sum
         for (int kb = 0; kb < nk && ok; ++kb) {
           const int      s  = kb % kStages;
           const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
@@ -189,11 +196,14 @@ namespace rg {
           tc_fence_after();
           const uint64_t da = smem_desc_sw128(sA + s * kBytesA);
           const uint64_t db = smem_desc_sw128(sB + s * kBytesB);
+          const uint32_t acc = kb < g.kb_lead ? 0u : 1u;
 #pragma unroll
           for (int k = 0; k < kBK / kUmmaK; ++k) {
             // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
-            mma_bf16(tmem_d, da + uint64_t(2 * k), db + uint64_t(2 * k), (kb > 0 || k > 0) ? 1u : 0u);
+            mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k),
+                     ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
           }
+          started |= 1u << acc;
           mma_commit(&empty_bar[s]);
         }
         mma_commit(&done_bar);
@@ -215,9 +225,19 @@ namespace rg {
       if (done && nk > 0) {
         const int row = m0 + warp * 32 + lane;
 #pragma unroll 1
+        const bool two = nk > g.kb_lead; // accumulator 1 was written
         for (int c = 0; c < kBN / 32; ++c) {
           float v[32];
-          tmem_ld32(tmem_d + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c * 32), v);
+          const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+          tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
+          if (two) {
+            float w[32];
+            tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(kBN + c * 32), w);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              v[j] += w[j];
+            }
+          }
           const int col0 = n0 + c * 32;
           if (row < g.M && col0 < g.N) {
             float* dst = g.C + static_cast<int64_t>(row) * g.ldc + col0;
@@ -572,6 +592,7 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
   g.M         = ndist;
   g.N         = pl->nbins;
   g.Kp        = pl->nterms * pl->gpad;
+  g.kb_lead   = pl->gpad / rg::kBK;
   g.C         = out;
   g.ldc       = pl->nbins;
   g.col_scale = pl->d_ebins;
@@ -596,6 +617,7 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
   g.M         = ndist;
   g.N         = pl->ng;
   g.Kp        = pl->nterms * pl->epad;
+  g.kb_lead   = pl->epad / rg::kBK;
   g.C         = grad_f;
   g.ldc       = pl->ng;
   g.col_scale = nullptr;

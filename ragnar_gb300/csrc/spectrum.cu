@@ -18,10 +18,13 @@
 //      segment table in shared memory whose entries past the last segment are
 //      zero, so an out-of-range x reads zero without a branch; the low 22 bits,
 //      read as a denormal, times the stored slope (pre-scaled by 2^127) give
-//      frac * slope in one FFMA.  Per eval: IADD, SHF, LOP, LDS.64, FFMA (F),
+//      frac * slope in one FFMA.  Per eval: IADD (T), SHF (segment, ALU pipe),
+//      IMAD (fraction bits = T - segment 2^22, FMA pipe), LDS.64, FFMA (F),
 //      FFMA (accumulate).
 //      smooth table: T >> frac (clamped to a zero entry) indexes cubic Hermite
-//      segments; tau = (T & mask) 2^-frac; three FFMAs evaluate the cubic.
+//      segments; the fraction bits read as a denormal times 2^126 give
+//      tau' = bits 2^-23 exactly (the coefficients are rescaled to tau' when
+//      staged), and three FFMAs evaluate the cubic.
 //  * Lanes own photon bins (32 consecutive bins per row, K rows per lane), warps
 //    own particles; per-warp FP32 register accumulators are folded into
 //    double-float accumulators after every chunk and flushed per warp to FP64
@@ -97,9 +100,7 @@ namespace rg {
           tab[i] = p.table[i];
         }
       } else {
-        for (int i = tid; i <= p.hseg; i += kThreads) {
-          htab[i] = p.htable[i];
-        }
+        stage_smooth_table(p, htab, tid, kThreads);
       }
       int32_t P[K];
 #pragma unroll
@@ -110,13 +111,10 @@ namespace rg {
       const int      stage_floats = p.nslots * kChunkPad;
       const uint32_t dead         = dead_coordinate(Pmin, p.L);
       const int      frac         = (MODE == kModeRef) ? kFrac : p.frac;
-      const uint32_t fmask        = (1u << frac) - 1u;
       const uint32_t hseg         = static_cast<uint32_t>(p.hseg);
-      const float    tau_scale    = p.tau_scale;
-      // seg = T >> kFrac as a high multiply by 2^(32 - kFrac) (at most 2^10 whatever
-      // opaque_zero holds, so seg < kRefEntries), fraction bits = T - seg * 2^kFrac
-      const uint32_t seg_mul = (1u << (32 - kFrac)) >> (p.opaque_zero & 31u);
-      const uint32_t seg_neg = (~p.opaque_zero) << kFrac;
+      // fraction bits = T - seg * 2^frac as an IMAD (FMA pipe) next to the segment
+      // shift (ALU pipe): the two integer pipes share the per-eval work
+      const uint32_t seg_neg = (~p.opaque_zero) << frac;
 
       int seg_hint = 0;
       if (tid == 0) {
@@ -196,15 +194,16 @@ namespace rg {
           for (int k = 0; k < K; ++k) {
             const uint32_t T = static_cast<uint32_t>(P[k]) - q;
             if (MODE == kModeRef) {
-              const uint32_t sg = __umulhi(T, seg_mul);
+              const uint32_t sg = T >> kFrac;
               const float2   c  = tab[sg];
               const float    m  = __uint_as_float(sg * seg_neg + T);
               const float    F  = __fmaf_rn(m, c.y, c.x);
               acc[k]         = __fmaf_rn(A, F, acc[k]);
             } else {
-              const float4 c   = htab[min(T >> frac, hseg)];
-              const float  tau = __uint2float_rn(T & fmask) * tau_scale;
-              const float  F   = __fmaf_rn(tau, __fmaf_rn(tau, __fmaf_rn(tau, c.w, c.z), c.y), c.x);
+              const uint32_t sg  = T >> frac;
+              const float4   c   = htab[min(sg, hseg)];
+              const float    tau = smooth_tau(sg * seg_neg + T);
+              const float    F   = __fmaf_rn(tau, __fmaf_rn(tau, __fmaf_rn(tau, c.w, c.z), c.y), c.x);
               acc[k]           = __fmaf_rn(A, F, acc[k]);
             }
           }

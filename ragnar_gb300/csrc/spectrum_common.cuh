@@ -57,10 +57,10 @@ namespace rg {
     double*        partials;     // [(grid + nseg) * nslices * kWarps * kSliceBins]
     int            nslices;
     unsigned*      status;
-    // Always 0 (zero-initialised with the struct).  The kernel builds its integer
-    // multipliers from it, so the compiler cannot fold them into shifts and masks:
-    // the per-eval coordinate arithmetic then runs as IMAD on the FMA pipe instead
-    // of on the half-rate integer ALU pipe.
+    // Always 0 (zero-initialised with the struct).  The kernel builds an integer
+    // multiplier from it, so the compiler cannot fold the multiply into a mask:
+    // part of the per-eval coordinate arithmetic then runs as IMAD on the FMA
+    // pipe instead of on the half-rate integer ALU pipe.
     uint32_t       opaque_zero;
   };
 
@@ -277,6 +277,24 @@ namespace rg {
         }
       }
     }
+  }
+
+  // Smooth-table segments staged in shared memory with the cubic's coefficients
+  // rescaled to the variable tau' = fraction bits * 2^-23 (tau = tau' 2^(23 - frac),
+  // frac in [12, 22]): c1 s, c2 s^2, c3 s^3 with s = 2^(23 - frac), all exact.
+  __device__ __forceinline__ void stage_smooth_table(const FusedParams& p, float4* htab, int tid,
+                                                     int nthreads) {
+    const float s1 = ldexpf(1.0f, 23 - p.frac), s2 = s1 * s1, s3 = s2 * s1;
+    for (int i = tid; i <= p.hseg; i += nthreads) {
+      const float4 c = p.htable[i];
+      htab[i]        = make_float4(c.x, c.y * s1, c.z * s2, c.w * s3);
+    }
+  }
+
+  // tau' from the fraction bits fb < 2^22: fb read as a denormal float is fb 2^-149
+  // exactly, and 2^126 times that is fb 2^-23, exactly (one FMUL, no conversion).
+  __device__ __forceinline__ float smooth_tau(uint32_t fb) {
+    return __uint_as_float(fb) * 0x1p126f;
   }
 
   __device__ __forceinline__ double* warp_partial(const FusedParams& p, int b, int seg, int slice,

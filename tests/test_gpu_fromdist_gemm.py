@@ -154,3 +154,20 @@ def test_arguments(gpu, oracle_lib):
         plan.run(f, out)
     plan.run(f[:0], out[:0])  # no distributions: nothing to do
     plan.check()
+
+
+def test_long_k_accumulation_stays_within_tolerance(gpu, oracle_lib):
+    """1024 gamma bins (6 x 1024 concatenated K, 384 MMA steps) on 1024 photon bins over
+    15 decades: the FP32 accumulation must still meet the spectrum tolerance."""
+    gb = oracle_lib.logspace(1.0, 1e6, 1024)
+    bins = oracle_lib.logspace(1e-2, 1e13, 1024)
+    rng = np.random.default_rng(505)
+    g = gb.astype(np.float64)[None, :]
+    p = rng.uniform(-3.0, -1.5, (256, 1))
+    lo = 10.0 ** rng.uniform(0.0, 2.0, (256, 1))
+    hi = 10.0 ** rng.uniform(3.0, 6.0, (256, 1))
+    f = np.where((g >= lo) & (g < hi), g**p, 0.0).astype(np.float32)
+    plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=256)
+    S = _run(plan, f, gpu).astype(np.float64)
+    S64 = (f.astype(np.float64) @ plan.kernel_matrix().T) * bins.astype(np.float64)[None, :]
+    assert _rows_max_rel(S, S64) <= SPECTRUM_RTOL
