@@ -57,10 +57,11 @@ def parse_args():
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm"],
+    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm", "histogram"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
-                         "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches")
+                         "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
+                         "energyDistribution of 3.3e7 particles into 200 log bins, 4 calls")
     return ap.parse_args()
 
 
@@ -731,7 +732,7 @@ def adam_fit_case(torch, capi, device, steps=200):
                                                                 np.max(np.abs(g64), axis=1, keepdims=True)))}
 
 
-def histogram_case(torch, capi, device, comps, n):
+def histogram_case(torch, capi, device, comps, n, reps=10):
     """Particles.energyDistribution of the dump-scale particles into 200 log gamma-beta
     bins 1e-2..1e3 (12 B/particle read: the HBM-bound kernel)."""
     import numpy as np  # noqa: PLC0415
@@ -745,7 +746,7 @@ def histogram_case(torch, capi, device, comps, n):
                                                      comps[2].data_ptr(), n, bins.ctypes.data, 200, 1, 1,
                                                      hist.data_ptr(), None, stream))
 
-    t = timed(torch, run, 10)
+    t = timed(torch, run, reps, warm=1)
     return {"particles": n, "bins": 200, "particles_per_s": n / t, "ms": t * 1e3,
             "hbm_gbs": 12.0 * n / t / 1e9}
 
@@ -797,6 +798,20 @@ def profile_gemm_case():
     print("profile gemm case done")
 
 
+def profile_histogram_case():
+    """4 energyDistribution calls on one dump-scale species (3.3e7 particles, 396 MB of u)."""
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    comps = make_particles(torch, N_PER_SPECIES, 1, device, seed=3)
+    for _ in range(4):
+        histogram_case(torch, capi, device, comps, N_PER_SPECIES, reps=1)
+    print("profile histogram case done")
+
+
 def main():
     args = parse_args()
     if args.profile_case == "spectrum":
@@ -804,6 +819,9 @@ def main():
         return
     if args.profile_case == "gemm":
         profile_gemm_case()
+        return
+    if args.profile_case == "histogram":
+        profile_histogram_case()
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

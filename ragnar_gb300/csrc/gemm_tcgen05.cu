@@ -7,8 +7,11 @@
 // many distributions f[d, g] give one GEMM:  S[d, e] = e * sum_g f[d, g] K[e, g].
 //
 // Precision: FP32 operands are split into BF16 terms (x = h + m + l, each the
-// BF16 rounding of the remainder) and the products are summed in one GEMM over
-// a concatenated K dimension, accumulated in FP32 in tensor memory:
+// BF16 rounding of the remainder; for FP32 input every step is exact in FP32)
+// stored side by side, [h | m | l] per row, and the products are summed in one
+// GEMM whose k loop walks (product, gamma block) pairs -- the TMA producer maps
+// product t to the stored terms it multiplies -- accumulated in FP32 in tensor
+// memory:
 //   6 products  (h.h + h.m + m.h + h.l + l.h + m.m): ~1e-8 relative per product (default)
 //   3 products  (h.h + h.m + m.h):                  ~1e-5 relative per product (fast)
 // The dominant h.h product accumulates in its own TMEM accumulator and the
@@ -52,6 +55,9 @@ namespace rg {
     constexpr uint32_t kBytesB = kBN * kBK * 2;
     constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
     constexpr unsigned kDevGemmTimeout = 8u;
+    // products h.h, h.m, m.h, h.l, l.h, m.m: stored term (0 h, 1 m, 2 l) of each operand
+    __constant__ int kLeft[6]  = { 0, 0, 1, 0, 2, 1 };
+    __constant__ int kRight[6] = { 0, 1, 0, 2, 0, 1 };
 
     __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y,
                                                 uint64_t* bar) {
@@ -123,8 +129,9 @@ namespace rg {
     }
 
     struct GemmArgs {
-      int          M, N, Kp; // Kp: concatenated K, a multiple of kBK
-      int          kb_lead;  // k blocks of the leading (h.h) product: accumulator 0
+      int          M, N;
+      int          kpt;      // k blocks per product (padded K / kBK)
+      int          nprod;    // products: 6 or 3 (the first is h.h, accumulator 0)
       float*       C;
       int          ldc;
       const float* col_scale; // nullable
@@ -145,7 +152,7 @@ namespace rg {
 
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
-      const int nk = g.Kp / kBK;
+      const int nk = g.nprod * g.kpt;
 
       if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -177,9 +184,11 @@ namespace rg {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
+          // product t = kb / kpt multiplies stored term kLeft[t] of A by kRight[t] of B
+          const int t = kb / g.kpt, gblk = kb - t * g.kpt;
           mbar_arrive_expect_tx(&full_bar[s], kBytesA + kBytesB);
-          tma_load_2d(sA + s * kBytesA, &tmA, kb * kBK, m0, &full_bar[s]);
-          tma_load_2d(sB + s * kBytesB, &tmB, kb * kBK, n0, &full_bar[s]);
+          tma_load_2d(sA + s * kBytesA, &tmA, (kLeft[t] * g.kpt + gblk) * kBK, m0, &full_bar[s]);
+          tma_load_2d(sB + s * kBytesB, &tmB, (kRight[t] * g.kpt + gblk) * kBK, n0, &full_bar[s]);
         }
       } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----------------------------------------------------------------
@@ -196,7 +205,7 @@ namespace rg {
           tc_fence_after();
           const uint64_t da = smem_desc_sw128(sA + s * kBytesA);
           const uint64_t db = smem_desc_sw128(sB + s * kBytesB);
-          const uint32_t acc = kb < g.kb_lead ? 0u : 1u;
+          const uint32_t acc = kb < g.kpt ? 0u : 1u;
 #pragma unroll
           for (int k = 0; k < kBK / kUmmaK; ++k) {
             // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
@@ -225,7 +234,7 @@ namespace rg {
       if (done && nk > 0) {
         const int row = m0 + warp * 32 + lane;
 #pragma unroll 1
-        const bool two = nk > g.kb_lead; // accumulator 1 was written
+        const bool two = nk > g.kpt; // accumulator 1 was written
         for (int c = 0; c < kBN / 32; ++c) {
           float v[32];
           const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
@@ -282,11 +291,21 @@ namespace rg {
       l         = __double2bfloat16(r);
     }
 
-    // dst[r][t * cpad + c] = term pattern[t] of src[r][c] * scale[c] (zero in the
-    // padding).  which = 0: left operand pattern, 1: right operand pattern.
+    // The same for an FP32 value: h is within a binade of v, so v - h and the next
+    // remainder are exact in FP32 (at most 17 significant bits).
+    __device__ __forceinline__ void split3f(float v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+      h       = __float2bfloat16_rn(v);
+      float r = __fsub_rn(v, __bfloat162float(h));
+      m       = __float2bfloat16_rn(r);
+      r       = __fsub_rn(r, __bfloat162float(m));
+      l       = __float2bfloat16_rn(r);
+    }
+
+    // dst[r][t * cpad + c] = term t (h, m, l; the first nstore) of src[r][c] * scale[c]
+    // (zero in the padding), FP32 throughout.
     __global__ void split_rows_kernel(const float* __restrict__ src, int rows, int cols, int ld,
                                       const float* __restrict__ col_scale, __nv_bfloat16* __restrict__ dst,
-                                      int cpad, int nterms, int which) {
+                                      int cpad, int nstore) {
       const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
       if (i >= static_cast<int64_t>(rows) * cpad) {
         return;
@@ -294,20 +313,17 @@ namespace rg {
       const int r = static_cast<int>(i / cpad), c = static_cast<int>(i % cpad);
       __nv_bfloat16 t[3];
       if (c < cols) {
-        double v = src[static_cast<int64_t>(r) * ld + c];
+        float v = src[static_cast<int64_t>(r) * ld + c];
         if (col_scale) {
-          v *= static_cast<double>(col_scale[c]);
+          v = __fmul_rn(v, col_scale[c]);
         }
-        split3(v, t[0], t[1], t[2]);
+        split3f(v, t[0], t[1], t[2]);
       } else {
         t[0] = t[1] = t[2] = __float2bfloat16(0.0f);
       }
-      // products (h,h) (h,m) (m,h) (h,l) (l,h) (m,m): left [h h m h l m], right [h m h l h m]
-      constexpr int left[6]  = { 0, 0, 1, 0, 2, 1 };
-      constexpr int right[6] = { 0, 1, 0, 2, 0, 1 };
-      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nterms * cpad;
-      for (int k = 0; k < nterms; ++k) {
-        row[k * cpad + c] = t[which ? right[k] : left[k]];
+      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nstore * cpad;
+      for (int k = 0; k < nstore; ++k) {
+        row[k * cpad + c] = t[k];
       }
     }
 
@@ -352,7 +368,7 @@ namespace rg {
     }
 
     __global__ void split_matrix_kernel(const double* __restrict__ K, int nbins, int ng, int transpose,
-                                        __nv_bfloat16* __restrict__ dst, int cpad, int nterms) {
+                                        __nv_bfloat16* __restrict__ dst, int cpad, int nstore) {
       // rows: e (cols g) or, transposed, g (cols e)
       const int     rows = transpose ? ng : nbins, cols = transpose ? nbins : ng;
       const int64_t i    = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -367,10 +383,9 @@ namespace rg {
       } else {
         t[0] = t[1] = t[2] = __float2bfloat16(0.0f);
       }
-      constexpr int right[6] = { 0, 1, 0, 2, 0, 1 };
-      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nterms * cpad;
-      for (int k = 0; k < nterms; ++k) {
-        row[k * cpad + c] = t[right[k]];
+      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nstore * cpad;
+      for (int k = 0; k < nstore; ++k) {
+        row[k * cpad + c] = t[k];
       }
     }
 
@@ -433,17 +448,18 @@ namespace rg {
 } // namespace rg
 
 struct rg_fromdist_plan {
-  int            ng = 0, nbins = 0, nterms = 6, max_dist = 0, log_spaced = 1, mode = RG_TABLE_REFERENCE;
+  int            ng = 0, nbins = 0, nprod = 6, nstore = 3, max_dist = 0, log_spaced = 1, mode = RG_TABLE_REFERENCE;
   int            gpad = 0, epad = 0; // padded K extents of the forward / adjoint GEMMs
   float          g_syn = 1, eps = 1;
   bool           zero  = false;
   float*         d_gbeta = nullptr;
   float*         d_ebins = nullptr; // photon energies with invalid bins set to 0
   double*        d_K     = nullptr; // nbins x ng kernel matrix (FP64)
-  __nv_bfloat16* d_B     = nullptr; // forward right operand  [nbins x nterms*gpad]
-  __nv_bfloat16* d_BT    = nullptr; // adjoint right operand  [ng x nterms*epad]
-  __nv_bfloat16* d_A     = nullptr; // forward left operand   [max_dist x nterms*gpad]
-  __nv_bfloat16* d_AT    = nullptr; // adjoint left operand   [max_dist x nterms*epad]
+  // BF16 terms [h | m | l] (the first nstore) per row
+  __nv_bfloat16* d_B     = nullptr; // forward right operand  [nbins x nstore*gpad]
+  __nv_bfloat16* d_BT    = nullptr; // adjoint right operand  [ng x nstore*epad]
+  __nv_bfloat16* d_A     = nullptr; // forward left operand   [max_dist x nstore*gpad]
+  __nv_bfloat16* d_AT    = nullptr; // adjoint left operand   [max_dist x nstore*epad]
   unsigned*      d_status = nullptr;
   CUtensorMap    tA, tB, tAT, tBT;
 };
@@ -467,7 +483,8 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
   auto pl        = std::make_unique<rg_fromdist_plan>();
   pl->ng         = ng;
   pl->nbins      = nbins;
-  pl->nterms     = split_products;
+  pl->nprod      = split_products;
+  pl->nstore     = split_products == 6 ? 3 : 2; // 3 products use h and m only
   pl->max_dist   = max_dist;
   pl->log_spaced = log_spaced ? 1 : 0;
   pl->mode       = table_mode;
@@ -501,7 +518,7 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
       return fail(rg::cuda_error(e_, #expr));                                               \
     }                                                                                       \
   } while (0)
-  const size_t kf = static_cast<size_t>(pl->nterms) * pl->gpad, ka = static_cast<size_t>(pl->nterms) * pl->epad;
+  const size_t kf = static_cast<size_t>(pl->nstore) * pl->gpad, ka = static_cast<size_t>(pl->nstore) * pl->epad;
   RG_PLAN_CUDA(cudaMalloc(&pl->d_gbeta, sizeof(float) * ng));
   RG_PLAN_CUDA(cudaMalloc(&pl->d_ebins, sizeof(float) * nbins));
   RG_PLAN_CUDA(cudaMalloc(&pl->d_K, sizeof(double) * nbins * ng));
@@ -542,10 +559,10 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
   }
   const int64_t nb = static_cast<int64_t>(nbins) * pl->gpad, nt = static_cast<int64_t>(ng) * pl->epad;
   rg::split_matrix_kernel<<<static_cast<unsigned>((nb + 255) / 256), 256>>>(pl->d_K, nbins, ng, 0, pl->d_B,
-                                                                            pl->gpad, pl->nterms);
+                                                                            pl->gpad, pl->nstore);
   RG_PLAN_CUDA(cudaGetLastError());
   rg::split_matrix_kernel<<<static_cast<unsigned>((nt + 255) / 256), 256>>>(pl->d_K, nbins, ng, 1, pl->d_BT,
-                                                                            pl->epad, pl->nterms);
+                                                                            pl->epad, pl->nstore);
   RG_PLAN_CUDA(cudaGetLastError());
   RG_PLAN_CUDA(cudaDeviceSynchronize());
   int st = rg::encode_tiled(&pl->tA, pl->d_A, kf, max_dist, rg::kBM);
@@ -586,13 +603,13 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
   auto          s  = static_cast<cudaStream_t>(stream);
   const int64_t nA = static_cast<int64_t>(ndist) * pl->gpad;
   rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
-    f, ndist, pl->ng, pl->ng, nullptr, pl->d_A, pl->gpad, pl->nterms, 0);
+    f, ndist, pl->ng, pl->ng, nullptr, pl->d_A, pl->gpad, pl->nstore);
   RG_CUDA_TRY(cudaGetLastError());
   rg::GemmArgs g {};
   g.M         = ndist;
   g.N         = pl->nbins;
-  g.Kp        = pl->nterms * pl->gpad;
-  g.kb_lead   = pl->gpad / rg::kBK;
+  g.kpt       = pl->gpad / rg::kBK;
+  g.nprod     = pl->nprod;
   g.C         = out;
   g.ldc       = pl->nbins;
   g.col_scale = pl->d_ebins;
@@ -611,13 +628,13 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
   const int64_t nA = static_cast<int64_t>(ndist) * pl->epad;
   // left operand: dL/dS[d][e] * e_e
   rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
-    grad_out, ndist, pl->nbins, pl->nbins, pl->d_ebins, pl->d_AT, pl->epad, pl->nterms, 0);
+    grad_out, ndist, pl->nbins, pl->nbins, pl->d_ebins, pl->d_AT, pl->epad, pl->nstore);
   RG_CUDA_TRY(cudaGetLastError());
   rg::GemmArgs g {};
   g.M         = ndist;
   g.N         = pl->ng;
-  g.Kp        = pl->nterms * pl->epad;
-  g.kb_lead   = pl->epad / rg::kBK;
+  g.kpt       = pl->epad / rg::kBK;
+  g.nprod     = pl->nprod;
   g.C         = grad_f;
   g.ldc       = pl->ng;
   g.col_scale = nullptr;

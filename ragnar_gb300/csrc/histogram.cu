@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <vector>
 
 namespace rg {
@@ -229,6 +230,50 @@ namespace rg {
       ref_energy_index(std::numeric_limits<float>::quiet_NaN(), fourvel, emin, emax, n));
   }
 
+  // Thresholds of recently used bin sets (the host binary search costs far more
+  // than the histogram kernel for small particle counts); keyed on the bin values
+  // and the energy definition, at most kThrCacheEntries kept.
+  struct ThrEntry {
+    std::vector<float> bins, thr;
+    bool               fourvel = true;
+    int                nan_index = 0;
+    float              emin = 0, emax = 0;
+  };
+
+  void cached_thresholds(const float* bins, int n, bool fourvel, std::vector<float>& thr, int& nan_index,
+                         float& emin, float& emax) {
+    constexpr std::size_t         kThrCacheEntries = 16;
+    static std::mutex             mu;
+    static std::vector<ThrEntry>  cache; // most recent last
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      for (auto it = cache.begin(); it != cache.end(); ++it) {
+        if (it->fourvel == fourvel && static_cast<int>(it->bins.size()) == n &&
+            std::memcmp(it->bins.data(), bins, sizeof(float) * n) == 0) {
+          thr       = it->thr;
+          nan_index = it->nan_index;
+          emin      = it->emin;
+          emax      = it->emax;
+          std::rotate(it, it + 1, cache.end());
+          return;
+        }
+      }
+    }
+    energy_thresholds(bins, n, fourvel, thr, nan_index, emin, emax);
+    ThrEntry e;
+    e.bins.assign(bins, bins + n);
+    e.thr       = thr;
+    e.fourvel   = fourvel;
+    e.nan_index = nan_index;
+    e.emin      = emin;
+    e.emax      = emax;
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache.size() >= kThrCacheEntries) {
+      cache.erase(cache.begin());
+    }
+    cache.push_back(std::move(e));
+  }
+
 } // namespace rg
 
 extern "C" {
@@ -263,7 +308,7 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
   std::vector<float> thr;
   int                nan_index = 0;
   float              emin, emax;
-  rg::energy_thresholds(bins, nbins, fourvel != 0, thr, nan_index, emin, emax);
+  rg::cached_thresholds(bins, nbins, fourvel != 0, thr, nan_index, emin, emax);
 
   rg::DeviceContext* ctx = nullptr;
   RG_TRY(rg::context(&ctx));
