@@ -642,6 +642,12 @@ def fromdist_gemm_case(torch, capi, device, peak_bf16):
     res = {"distributions": nd, "gamma_bins": ng, "photon_bins": ne}
     for terms in (6, 3):
         plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=nd, split_products=terms)
+        tuned = plan.config()
+        shapes = {}
+        for cfg, (bn, stages) in enumerate([(256, 4), (128, 6), (128, 3)]):
+            plan.set_config(cfg, -1)
+            shapes[f"128x{bn}_s{stages}_ms"] = timed(torch, lambda: plan.run(f, out, stream), 10) * 1e3
+        plan.set_config([(256, 4), (128, 6), (128, 3)].index(tuned["fwd"]), -1)
         t = timed(torch, lambda: plan.run(f, out, stream), 20)
         plan.check(stream)
         K = plan.kernel_matrix()
@@ -652,7 +658,8 @@ def fromdist_gemm_case(torch, capi, device, peak_bf16):
         flops = 2.0 * nd * ng * ne * terms
         res[f"bf16x{terms}"] = {
             "evals_per_s": nd * ng * ne / t, "ms": t * 1e3, "bf16_tflops": flops / t / 1e12,
-            "frac_of_bf16_peak": flops / t / 1e12 / peak_bf16, "max_rel_err_vs_fp64": err}
+            "frac_of_bf16_peak": flops / t / 1e12 / peak_bf16, "max_rel_err_vs_fp64": err,
+            "autotuned_tile": {"fwd": list(tuned["fwd"]), "adj": list(tuned["adj"])}, "tile_timings": shapes}
         plan.close()
     res["peak_bf16_tflops"] = peak_bf16
     return res

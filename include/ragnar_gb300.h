@@ -254,8 +254,9 @@ typedef struct rg_fromdist_plan rg_fromdist_plan;
  * gbeta (host, ng) give S[d][e] = e * sum_g K[e][g] f[d][g] with the kernel
  * matrix K[e][g] = J_g F(e / e_peak(g)) (built once here, FP64).  The product
  * runs as one BF16 tensor-core GEMM (tcgen05) over split-precision operands:
- * split_products = 6 (three BF16 terms per operand, ~1e-8 relative) or 3 (two
- * terms, ~1e-5 relative).  bins is host (nbins).  Either table mode.
+ * split_products = 6 (three BF16 terms per operand, ~1e-8 relative per product)
+ * or 3 (two terms, ~1e-5 relative).  bins is host (nbins).  Either table mode.
+ * Creation builds K, splits it and autotunes the GEMM tile shape (synchronous).
  * Extension: the reference handles one distribution per call. */
 int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, const float* bins, int32_t nbins,
                             float g_syn, float e_syn_at_g_syn, int32_t table_mode, int32_t split_products,
@@ -271,6 +272,16 @@ int rg_fromdist_adjoint(rg_fromdist_plan* plan, const float* grad_out, int32_t n
 
 /* Synchronises `stream`; RG_ERR_TIMEOUT if a bounded wait in the GEMM gave up. */
 int rg_fromdist_plan_check(rg_fromdist_plan* plan, void* stream);
+
+/* Tile shape of the forward and adjoint GEMMs: chosen at plan creation by timing
+ * every supported shape (CTA tile 128 x bn, a TMA ring of `stages` k blocks) on
+ * the plan's own sizes, cached per device and shape.  No reference counterpart. */
+int rg_fromdist_plan_config(const rg_fromdist_plan* plan, int32_t* fwd_bn, int32_t* fwd_stages,
+                            int32_t* adj_bn, int32_t* adj_stages);
+
+/* Overrides the tuned shapes with entries 0..2 of the supported list
+ * ((256, 4), (128, 6), (128, 3)); -1 keeps the current choice. */
+int rg_fromdist_plan_set_config(rg_fromdist_plan* plan, int32_t fwd_cfg, int32_t adj_cfg);
 
 /* Copies the FP64 kernel matrix K (nbins x ng) to host memory. */
 int rg_fromdist_kernel_matrix(rg_fromdist_plan* plan, double* K_host);

@@ -102,6 +102,9 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_fromdist_adjoint": [_vp, _vp, _i32, _vp, _vp],
         "rg_fromdist_plan_check": [_vp, _vp],
         "rg_fromdist_kernel_matrix": [_vp, _vp],
+        "rg_fromdist_plan_config": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                    ctypes.POINTER(_i32)],
+        "rg_fromdist_plan_set_config": [_vp, _i32, _i32],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
         "rg_smooth_table": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
                             ctypes.POINTER(ctypes.c_double)],
@@ -285,6 +288,15 @@ class FromDistPlan:
 
     def check(self, stream: int = 0) -> None:
         check(lib().rg_fromdist_plan_check(self.handle, stream))
+
+    def config(self) -> dict:
+        """Autotuned tile shapes {"fwd": (bn, stages), "adj": (bn, stages)}."""
+        v = [_i32() for _ in range(4)]
+        check(lib().rg_fromdist_plan_config(self.handle, *[ctypes.byref(x) for x in v]))
+        return {"fwd": (v[0].value, v[1].value), "adj": (v[2].value, v[3].value)}
+
+    def set_config(self, fwd: int = -1, adj: int = -1) -> None:
+        check(lib().rg_fromdist_plan_set_config(self.handle, fwd, adj))
 
     def kernel_matrix(self):
         import numpy as np  # noqa: PLC0415

@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <vector>
@@ -46,14 +47,18 @@ namespace rg {
   namespace {
 
     constexpr int kBM       = 128;
-    constexpr int kBN       = 256;
     constexpr int kBK       = 64; // bf16 elements = 128 bytes: one swizzle row
-    constexpr int kStages   = 4;
     constexpr int kUmmaK    = 16;
     constexpr int kGemmThreads = 128;
     constexpr uint32_t kBytesA = kBM * kBK * 2;
-    constexpr uint32_t kBytesB = kBN * kBK * 2;
-    constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
+
+    // Tile shapes the autotuner chooses from: N width of the CTA tile (M is 128)
+    // and the depth of the TMA ring.  Two FP32 accumulators of `bn` TMEM columns.
+    struct GemmConfig {
+      int bn, stages;
+    };
+    constexpr GemmConfig kConfigs[] = { { 256, 4 }, { 128, 6 }, { 128, 3 } };
+    constexpr int        kNumConfigs = 3;
     constexpr unsigned kDevGemmTimeout = 8u;
     // products h.h, h.m, m.h, h.l, l.h, m.m: stored term (0 h, 1 m, 2 l) of each operand
     __constant__ int kLeft[6]  = { 0, 0, 1, 0, 2, 1 };
@@ -82,15 +87,18 @@ namespace rg {
     }
 
     // Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major,
-    // N = 256, M = 128.
-    constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kBN >> 3) << 17) |
-                                (uint32_t(kBM >> 4) << 24);
+    // N = bn, M = 128.
+    template <int BN>
+    constexpr uint32_t idesc() {
+      return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(kBM >> 4) << 24);
+    }
 
-    __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                             uint32_t accumulate) {
       asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
     }
 
@@ -138,9 +146,13 @@ namespace rg {
       unsigned*    status;
     };
 
+    template <int kBN, int kStages>
     __global__ void __launch_bounds__(kGemmThreads, 1)
       gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                           const __grid_constant__ GemmArgs g) {
+      constexpr uint32_t kBytesB   = kBN * kBK * 2;
+      constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
+      constexpr uint32_t kIdesc    = idesc<kBN>();
       extern __shared__ __align__(1024) unsigned char smem_raw[];
       // 1024-byte alignment of the swizzled stage buffers
       unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -209,7 +221,7 @@ namespace rg {
 #pragma unroll
           for (int k = 0; k < kBK / kUmmaK; ++k) {
             // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
-            mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k),
+            mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k), kIdesc,
                      ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
           }
           started |= 1u << acc;
@@ -419,24 +431,45 @@ namespace rg {
       return RG_OK;
     }
 
-    size_t gemm_smem() {
-      return kStages * (kBytesA + kBytesB) + 1024;
+    size_t gemm_smem(int cfg) {
+      return static_cast<size_t>(kConfigs[cfg].stages) * (kBytesA + kConfigs[cfg].bn * kBK * 2) + 1024;
     }
 
-    int launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+    template <int BN, int STAGES>
+    int launch_gemm_t(int cfg, const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
       static bool configured = false;
       if (!configured) {
-        RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(gemm_smem())));
+        RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, STAGES>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(gemm_smem(cfg))));
         configured = true;
       }
+      const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM);
+      gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg), s>>>(tA, tB, g);
+      RG_CUDA_TRY(cudaGetLastError());
+      return RG_OK;
+    }
+
+    // tB is the right operand's tensor map whose box height is the config's bn.
+    int launch_gemm(int cfg, const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
       if (g.M <= 0 || g.N <= 0) {
         return RG_OK;
       }
-      const dim3 grid((g.N + kBN - 1) / kBN, (g.M + kBM - 1) / kBM);
-      gemm_bf16_tn_kernel<<<grid, kGemmThreads, gemm_smem(), s>>>(tA, tB, g);
-      RG_CUDA_TRY(cudaGetLastError());
-      return RG_OK;
+      switch (cfg) {
+        case 0:
+          return launch_gemm_t<kConfigs[0].bn, kConfigs[0].stages>(0, tA, tB, g, s);
+        case 1:
+          return launch_gemm_t<kConfigs[1].bn, kConfigs[1].stages>(1, tA, tB, g, s);
+        case 2:
+          return launch_gemm_t<kConfigs[2].bn, kConfigs[2].stages>(2, tA, tB, g, s);
+        default:
+          return set_error(RG_ERR_ARGUMENT, "unknown GEMM configuration");
+      }
+    }
+
+    // Box height index of a config's right-operand tensor map: 0 for bn 256, 1 for 128.
+    int box_index(int cfg) {
+      return kConfigs[cfg].bn == 256 ? 0 : 1;
     }
 
     int round_up(int v, int m) {
@@ -461,8 +494,108 @@ struct rg_fromdist_plan {
   __nv_bfloat16* d_A     = nullptr; // forward left operand   [max_dist x nstore*gpad]
   __nv_bfloat16* d_AT    = nullptr; // adjoint left operand   [max_dist x nstore*epad]
   unsigned*      d_status = nullptr;
-  CUtensorMap    tA, tB, tAT, tBT;
+  CUtensorMap    tA, tAT;
+  CUtensorMap    tB[2], tBT[2]; // right operands with box height 256 and 128
+  int            cfg_fwd = 0, cfg_adj = 0; // autotuned tile shapes
 };
+
+namespace rg {
+
+  namespace {
+
+    // Times every tile shape on the plan's own GEMM (max_dist rows, zero left
+    // operand) and returns the fastest; results are cached per device and shape.
+    int tune_gemm(rg_fromdist_plan* pl, bool adjoint, int* best_cfg) {
+      static std::mutex                            mu;
+      static std::map<std::vector<int>, int>       cache;
+      int dev = 0;
+      RG_CUDA_TRY(cudaGetDevice(&dev));
+      GemmArgs g {};
+      g.M         = pl->max_dist;
+      g.N         = adjoint ? pl->ng : pl->nbins;
+      g.kpt       = (adjoint ? pl->epad : pl->gpad) / kBK;
+      g.nprod     = pl->nprod;
+      g.ldc       = g.N;
+      g.col_scale = adjoint ? nullptr : pl->d_ebins;
+      g.status    = pl->d_status;
+      const std::vector<int> key { dev, adjoint ? 1 : 0, g.M, g.N, g.kpt, g.nprod };
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) {
+          *best_cfg = it->second;
+          return RG_OK;
+        }
+      }
+      float*      C  = nullptr;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      auto cleanup = [&]() {
+        cudaFree(C);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+      };
+      auto fail = [&](int st) {
+        cleanup();
+        return st;
+      };
+      cudaError_t e = cudaMalloc(&C, sizeof(float) * static_cast<size_t>(g.M) * g.N);
+      if (e == cudaSuccess) e = cudaEventCreate(&e0);
+      if (e == cudaSuccess) e = cudaEventCreate(&e1);
+      const size_t abytes = sizeof(__nv_bfloat16) * static_cast<size_t>(pl->max_dist) * pl->nstore *
+                            (adjoint ? pl->epad : pl->gpad);
+      if (e == cudaSuccess) e = cudaMemset(adjoint ? pl->d_AT : pl->d_A, 0, abytes);
+      if (e != cudaSuccess) {
+        return fail(cuda_error(e, "GEMM autotuning setup"));
+      }
+      g.C        = C;
+      int   best = 0;
+      float best_ms = 0.0f;
+      for (int cfg = 0; cfg < kNumConfigs; ++cfg) {
+        const CUtensorMap& tA = adjoint ? pl->tAT : pl->tA;
+        const CUtensorMap& tB = adjoint ? pl->tBT[box_index(cfg)] : pl->tB[box_index(cfg)];
+        for (int r = 0; r < 2; ++r) {
+          const int st = launch_gemm(cfg, tA, tB, g, nullptr);
+          if (st != RG_OK) {
+            return fail(st);
+          }
+        }
+        e = cudaEventRecord(e0, nullptr);
+        for (int r = 0; r < 5 && e == cudaSuccess; ++r) {
+          const int st = launch_gemm(cfg, tA, tB, g, nullptr);
+          if (st != RG_OK) {
+            return fail(st);
+          }
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+          return fail(cuda_error(e, "GEMM autotuning"));
+        }
+        if (cfg == 0 || ms < best_ms) {
+          best    = cfg;
+          best_ms = ms;
+        }
+      }
+      unsigned st = 0;
+      e = cudaMemcpy(&st, pl->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        return fail(cuda_error(e, "GEMM autotuning status"));
+      }
+      cleanup();
+      if (st != 0) {
+        return set_error(RG_ERR_TIMEOUT, "a bounded wait in the tensor-core GEMM gave up during autotuning");
+      }
+      std::lock_guard<std::mutex> lock(mu);
+      cache[key] = best;
+      *best_cfg  = best;
+      return RG_OK;
+    }
+
+  } // namespace
+
+} // namespace rg
 
 extern "C" {
 
@@ -566,9 +699,14 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
   RG_PLAN_CUDA(cudaGetLastError());
   RG_PLAN_CUDA(cudaDeviceSynchronize());
   int st = rg::encode_tiled(&pl->tA, pl->d_A, kf, max_dist, rg::kBM);
-  if (st == RG_OK) st = rg::encode_tiled(&pl->tB, pl->d_B, kf, nbins, rg::kBN);
   if (st == RG_OK) st = rg::encode_tiled(&pl->tAT, pl->d_AT, ka, max_dist, rg::kBM);
-  if (st == RG_OK) st = rg::encode_tiled(&pl->tBT, pl->d_BT, ka, ng, rg::kBN);
+  for (int b = 0; b < 2 && st == RG_OK; ++b) {
+    const uint32_t box = b == 0 ? 256u : 128u;
+    st = rg::encode_tiled(&pl->tB[b], pl->d_B, kf, nbins, box);
+    if (st == RG_OK) st = rg::encode_tiled(&pl->tBT[b], pl->d_BT, ka, ng, box);
+  }
+  if (st == RG_OK) st = rg::tune_gemm(pl.get(), false, &pl->cfg_fwd);
+  if (st == RG_OK) st = rg::tune_gemm(pl.get(), true, &pl->cfg_adj);
   if (st != RG_OK) {
     return fail(st);
   }
@@ -614,7 +752,7 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
   g.ldc       = pl->nbins;
   g.col_scale = pl->d_ebins;
   g.status    = pl->d_status;
-  return rg::launch_gemm(pl->tA, pl->tB, g, s);
+  return rg::launch_gemm(pl->cfg_fwd, pl->tA, pl->tB[rg::box_index(pl->cfg_fwd)], g, s);
 }
 
 int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndist, float* grad_f, void* stream) {
@@ -639,7 +777,7 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
   g.ldc       = pl->ng;
   g.col_scale = nullptr;
   g.status    = pl->d_status;
-  return rg::launch_gemm(pl->tAT, pl->tBT, g, s);
+  return rg::launch_gemm(pl->cfg_adj, pl->tAT, pl->tBT[rg::box_index(pl->cfg_adj)], g, s);
 }
 
 int rg_fromdist_plan_check(rg_fromdist_plan* pl, void* stream) {
@@ -654,6 +792,27 @@ int rg_fromdist_plan_check(rg_fromdist_plan* pl, void* stream) {
     RG_CUDA_TRY(cudaMemset(pl->d_status, 0, sizeof(unsigned)));
     return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait in the tensor-core GEMM gave up; results are invalid");
   }
+  return RG_OK;
+}
+
+int rg_fromdist_plan_config(const rg_fromdist_plan* pl, int32_t* fwd_bn, int32_t* fwd_stages, int32_t* adj_bn,
+                            int32_t* adj_stages) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  if (fwd_bn) *fwd_bn = rg::kConfigs[pl->cfg_fwd].bn;
+  if (fwd_stages) *fwd_stages = rg::kConfigs[pl->cfg_fwd].stages;
+  if (adj_bn) *adj_bn = rg::kConfigs[pl->cfg_adj].bn;
+  if (adj_stages) *adj_stages = rg::kConfigs[pl->cfg_adj].stages;
+  return RG_OK;
+}
+
+int rg_fromdist_plan_set_config(rg_fromdist_plan* pl, int32_t fwd_cfg, int32_t adj_cfg) {
+  if (!pl || fwd_cfg >= rg::kNumConfigs || adj_cfg >= rg::kNumConfigs) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_plan_set_config: configuration index out of range");
+  }
+  if (fwd_cfg >= 0) pl->cfg_fwd = fwd_cfg;
+  if (adj_cfg >= 0) pl->cfg_adj = adj_cfg;
   return RG_OK;
 }
 

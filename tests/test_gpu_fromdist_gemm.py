@@ -171,3 +171,26 @@ def test_long_k_accumulation_stays_within_tolerance(gpu, oracle_lib):
     S = _run(plan, f, gpu).astype(np.float64)
     S64 = (f.astype(np.float64) @ plan.kernel_matrix().T) * bins.astype(np.float64)[None, :]
     assert _rows_max_rel(S, S64) <= SPECTRUM_RTOL
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_every_tile_shape(gpu, oracle_lib, table, cfg):
+    """Each shape the autotuner may pick, forced, on sizes with partial tiles in M and N."""
+    gb = oracle_lib.logspace(1.0, 1e4, 300)
+    bins = oracle_lib.logspace(0.1, 1e9, 300)
+    f = _dists(gb, 200, seed=40 + cfg)
+    plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=200)
+    tuned = plan.config()
+    assert tuned["fwd"] in [(256, 4), (128, 6), (128, 3)] and tuned["adj"] in [(256, 4), (128, 6), (128, 3)]
+    plan.set_config(cfg, cfg)
+    S = _run(plan, f, gpu)
+    S64 = oracle_lib.sync_from_dist_f64(gb, f, True, bins, 1.0, 1.0, table)
+    assert _rows_max_rel(S, S64) <= SPECTRUM_RTOL
+    gS = np.random.default_rng(cfg).standard_normal((200, 300)).astype(np.float32)
+    gf = torch.empty((200, 300), device=gpu)
+    plan.adjoint(torch.from_numpy(gS).to(gpu), gf)
+    plan.check()
+    want = (gS.astype(np.float64) * bins.astype(np.float64)[None, :]) @ plan.kernel_matrix()
+    assert np.max(np.abs(gf.cpu().numpy() - want) / np.max(np.abs(want), axis=1, keepdims=True)) < 1e-5
+    with pytest.raises(capi.RgError, match="out of range"):
+        plan.set_config(3, 0)
