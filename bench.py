@@ -449,6 +449,7 @@ def run_ours(args, rank, world, local_rank):
         extra["fromdist_gemm_4096x1024x1024"] = guarded(fromdist_gemm_case, torch, capi, device, peak_bf16)
         extra["fromdist_gemm_4096x1024x1024"]["peak_source"] = peak_src
         extra["adam_fit_1024x512x512"] = guarded(adam_fit_case, torch, capi, device)
+        extra["ic_1024x1024x1024"] = guarded(ic_case, torch, capi, device, clocks.get("sm_mhz") or 2070.0)
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     result["extra"] = extra
@@ -737,6 +738,36 @@ def adam_fit_case(torch, capi, device, steps=200):
             "fwd_max_rel_err_vs_fp64": float(np.max(np.abs(Sg[mm] - S64[mm]) / S64[mm])),
             "grad_max_err_vs_fp64_rel_to_row_max": float(np.max(np.abs(gg - g64) /
                                                                 np.max(np.abs(g64), axis=1, keepdims=True)))}
+
+
+def ic_case(torch, capi, device, clk_mhz=2070.0):
+    """ICSpectrum of a 1024-bin particle power law (index -2 on [1e2, 1e7], exp cutoff at
+    3e6) on a 1024-bin soft-photon field (1e-9..1e-3 mec2, dN/dE ~ E^-1) into 1024 IC bins
+    1e-3..1e7: 1.07e9 (gamma, soft photon, IC bin) evals.  Bound: one MUFU lg2 per eval
+    (16 per SM per clock)."""
+    import numpy as np  # noqa: PLC0415
+
+    n = 1024
+    gb = logbins(capi, 1e2, 1e7, n)
+    fp = (gb.astype(np.float64) ** -2.0 * np.exp(-gb / 3e6)).astype(np.float32)
+    es = logbins(capi, 1e-9, 1e-3, n)
+    fs = (1.0 / es.astype(np.float64)).astype(np.float32)
+    eic = logbins(capi, 1e-3, 1e7, n)
+    t = [torch.from_numpy(a).to(device) for a in (gb, fp, es, fs, eic)]
+    out = torch.empty(n, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+
+    def run():
+        capi.check(capi.lib().rg_ic_spectrum(t[0].data_ptr(), t[1].data_ptr(), n, 1, t[2].data_ptr(),
+                                             t[3].data_ptr(), n, t[4].data_ptr(), n, out.data_ptr(), stream))
+
+    dt = timed(torch, run, 10)
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    evals = float(n) ** 3
+    peak = sms * 16 * clk_mhz * 1e6
+    return {"gamma_bins": n, "soft_photon_bins": n, "ic_bins": n, "ms": dt * 1e3, "evals_per_s": evals / dt,
+            "mufu_peak_evals_per_s": peak, "frac_of_mufu_peak": evals / dt / peak,
+            "finite": bool(torch.isfinite(out).all())}
 
 
 def histogram_case(torch, capi, device, comps, n, reps=10):

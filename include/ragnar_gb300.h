@@ -287,6 +287,19 @@ int rg_fromdist_plan_set_config(rg_fromdist_plan* plan, int32_t fwd_cfg, int32_t
 int rg_fromdist_kernel_matrix(rg_fromdist_plan* plan, double* K_host);
 
 /* --------------------------------------------------------------------------
+ * Inverse-Compton spectrum
+ * ------------------------------------------------------------------------ */
+
+/* ICSpectrum (ic.cpp:15-46; ic::Kernel ic.hpp:67-94, KNfunc ic.hpp:20-25):
+ * out[e] = sum_g sum_s f[g] (fs[s] / es[s]) eic[e]^2 KN(4 g es[s], q) / g^k over the pairs
+ * with eic[e] <= g Gamma / (1 + Gamma), k = 1 for log-spaced gamma bins (log_spaced != 0)
+ * and 2 otherwise.  All arrays are device arrays: gbins, f (ng), es, fs (ns), eic, out
+ * (ne).  Non-positive IC bins give 0 (the reference yields NaN there).  Units are the
+ * caller's to check (the reference requires mec^2 for es and eic). */
+int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_spaced, const float* es,
+                   const float* fs, int32_t ns, const float* eic, int32_t ne, float* out, void* stream);
+
+/* --------------------------------------------------------------------------
  * Energy distribution (histogram)
  * ------------------------------------------------------------------------ */
 

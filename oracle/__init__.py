@@ -75,6 +75,9 @@ def _declare(L: ctypes.CDLL) -> None:
     sm = [_i64, _f32p, _i64, _d, _d, _d, _f32p, _i64, _d, _d]
     L.orc_sync_smooth_f64.argtypes = D10 + sm + [_f64p, _int]
     L.orc_sync_smooth_grad_f64.argtypes = D10 + sm + [_f64p, _f64p, _f64p, _f64p, _f64p, _int]
+    ic = [_f32p, _f32p, _i64, _int, _f32p, _f32p, _i64, _f32p, _i64]
+    L.orc_ic_spectrum_ref32.argtypes = ic + [_f32p, _int]
+    L.orc_ic_spectrum_f64.argtypes = ic + [_f64p, _int]
 
 
 def _p(a, ptype=_f32p):
@@ -261,3 +264,27 @@ def sync_smooth_grad_f64(prt: dict, bins, B0, g_syn, eps, coef, gS, xmin=SMOOTH_
                                    eps, _p(coef), nseg, lnx, dln, _p(gS, _f64p), _p(gw, _f64p),
                                    _p(gu[0], _f64p), _p(gu[1], _f64p), _p(gu[2], _f64p), nthreads)
     return gw, gu
+
+
+# ---- inverse Compton --------------------------------------------------------------------
+
+def _ic_args(gb, fp, log_spaced, es, fs, eic):
+    gb, fp, es, fs, eic = (_f32arr(a) for a in (gb, fp, es, fs, eic))
+    return [_p(gb), _p(fp), len(gb), int(log_spaced), _p(es), _p(fs), len(es), _p(eic), len(eic)], len(eic), \
+        (gb, fp, es, fs, eic)
+
+
+def ic_spectrum_ref32(gb, fp, log_spaced, es, fs, eic, nthreads=0) -> np.ndarray:
+    """ICSpectrum (ic.cpp:15-46) with the reference's float arithmetic and reduction order."""
+    args, ne, keep = _ic_args(gb, fp, log_spaced, es, fs, eic)
+    out = np.empty(ne, np.float32)
+    lib().orc_ic_spectrum_ref32(*args, _p(out), nthreads)
+    return out
+
+
+def ic_spectrum_f64(gb, fp, log_spaced, es, fs, eic, nthreads=0) -> np.ndarray:
+    """FP64 ground truth of the IC spectrum E^2 dN/dE."""
+    args, ne, keep = _ic_args(gb, fp, log_spaced, es, fs, eic)
+    out = np.empty(ne, np.float64)
+    lib().orc_ic_spectrum_f64(*args, _p(out, _f64p), nthreads)
+    return out

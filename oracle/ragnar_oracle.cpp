@@ -697,3 +697,92 @@ void orc_sync_smooth_grad_f64(const double* ux, const double* uy, const double* 
 }
 
 } // extern "C"
+
+// ---- inverse Compton (physics/ic.hpp:20-95, physics/ic.cpp:15-46) ----------------------
+
+namespace {
+
+  // ic.hpp:20-25 (KNfunc) with the reference's type promotions: 2 q log(q) in float
+  // (logf), 0.5 Gq Gq / (1 + Gq) in double (0.5 is a double literal), the whole
+  // expression in double, returned as float.
+  float ic_kn_ref32(float Gamma, float q) {
+    const float  Gq    = Gamma * q;
+    const float  a     = 2 * q * std::log(q);
+    const double inner = static_cast<double>(1 + 2 * q) + 0.5 * Gq * Gq / static_cast<double>(1 + Gq);
+    return static_cast<float>(static_cast<double>(a) + static_cast<double>(1 - q) * inner);
+  }
+
+  double ic_kn_f64(double Gamma, double q) {
+    const double Gq = Gamma * q;
+    return 2.0 * q * std::log(q) + (1.0 - q) * ((1.0 + 2.0 * q) + 0.5 * Gq * Gq / (1.0 + Gq));
+  }
+
+} // namespace
+
+extern "C" {
+
+// ic.cpp:15-46: MDRange (gamma bin, soft-photon bin, IC bin) running ic::Kernel
+// (ic.hpp:67-94) into a ScatterView; float arithmetic as the reference writes it,
+// OpenMP static schedule over the collapsed index space with per-thread copies
+// summed in thread order (the Kokkos-API shim's ScatterDuplicated behaviour).
+void orc_ic_spectrum_ref32(const float* gb, const float* fp, std::int64_t ng, int log_spaced,
+                           const float* es, const float* fs, std::int64_t ns, const float* eic,
+                           std::int64_t ne, float* out, int nthreads) {
+  const int          nth = threads_or_default(nthreads);
+  std::vector<float> dup(static_cast<std::size_t>(nth) * ne, 0.0f);
+#pragma omp parallel for collapse(3) schedule(static) num_threads(nth)
+  for (std::int64_t g = 0; g < ng; ++g) {
+    for (std::int64_t s = 0; s < ns; ++s) {
+      for (std::int64_t e = 0; e < ne; ++e) {
+        const float g_prtls = gb[g], f_prtls = fp[g];
+        const float e_soft = es[s], f_soft = fs[s];
+        const float e_ic   = eic[e];
+        const float Gamma  = 4 * g_prtls * e_soft;
+        if (e_ic > g_prtls * Gamma / (1 + Gamma)) {
+          continue;
+        }
+        const float q  = (e_ic / g_prtls) / (Gamma * (1 - (e_ic / g_prtls)));
+        const float kn = ic_kn_ref32(Gamma, q);
+        const float v  = log_spaced ? f_prtls * (f_soft / e_soft) * e_ic * e_ic * kn / g_prtls
+                                    : f_prtls * (f_soft / e_soft) * e_ic * e_ic * kn / (g_prtls * g_prtls);
+        dup[static_cast<std::size_t>(omp_get_thread_num()) * ne + e] += v;
+      }
+    }
+  }
+  for (std::int64_t e = 0; e < ne; ++e) {
+    float acc = 0.0f;
+    for (int t = 0; t < nth; ++t) {
+      acc += dup[static_cast<std::size_t>(t) * ne + e];
+    }
+    out[e] = acc;
+  }
+}
+
+// FP64 ground truth of the same sum (inputs are the float arrays).
+void orc_ic_spectrum_f64(const float* gb, const float* fp, std::int64_t ng, int log_spaced,
+                         const float* es, const float* fs, std::int64_t ns, const float* eic,
+                         std::int64_t ne, double* out, int nthreads) {
+  const int nth = threads_or_default(nthreads);
+#pragma omp parallel for schedule(static) num_threads(nth)
+  for (std::int64_t e = 0; e < ne; ++e) {
+    const double e_ic = eic[e];
+    double       acc  = 0.0;
+    for (std::int64_t g = 0; g < ng; ++g) {
+      const double g_prtls = gb[g], f_prtls = fp[g];
+      for (std::int64_t s = 0; s < ns; ++s) {
+        const double e_soft = es[s], f_soft = fs[s];
+        const double Gamma  = 4.0 * g_prtls * e_soft;
+        if (e_ic > g_prtls * Gamma / (1.0 + Gamma)) {
+          continue;
+        }
+        const double r  = e_ic / g_prtls;
+        const double q  = r / (Gamma * (1.0 - r));
+        const double kn = ic_kn_f64(Gamma, q);
+        acc += f_prtls * (f_soft / e_soft) * e_ic * e_ic * kn / (log_spaced ? g_prtls : g_prtls * g_prtls);
+      }
+    }
+    out[e] = acc;
+  }
+}
+
+} // extern "C"

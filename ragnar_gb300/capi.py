@@ -105,6 +105,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_fromdist_plan_config": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                                     ctypes.POINTER(_i32)],
         "rg_fromdist_plan_set_config": [_vp, _i32, _i32],
+        "rg_ic_spectrum": [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
         "rg_smooth_table": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
                             ctypes.POINTER(ctypes.c_double)],

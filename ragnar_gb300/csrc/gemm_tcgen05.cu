@@ -314,29 +314,45 @@ namespace rg {
     }
 
     // dst[r][t * cpad + c] = term t (h, m, l; the first nstore) of src[r][c] * scale[c]
-    // (zero in the padding), FP32 throughout.
+    // (zero in the padding), FP32 throughout.  Thread = 4 consecutive columns of one
+    // row (cpad is a multiple of 64, so every 4-column group is inside the row and
+    // each term's 4 BF16 values are one aligned 8-byte store); rows stride by gridDim.y.
     __global__ void split_rows_kernel(const float* __restrict__ src, int rows, int cols, int ld,
                                       const float* __restrict__ col_scale, __nv_bfloat16* __restrict__ dst,
                                       int cpad, int nstore) {
-      const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (i >= static_cast<int64_t>(rows) * cpad) {
+      const int c0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+      if (c0 >= cpad) {
         return;
       }
-      const int r = static_cast<int>(i / cpad), c = static_cast<int>(i % cpad);
-      __nv_bfloat16 t[3];
-      if (c < cols) {
-        float v = src[static_cast<int64_t>(r) * ld + c];
-        if (col_scale) {
-          v = __fmul_rn(v, col_scale[c]);
+      for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+        const float* srow = src + static_cast<int64_t>(r) * ld;
+        __nv_bfloat16 t[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int c = c0 + j;
+          float     v = 0.0f;
+          if (c < cols) {
+            v = srow[c];
+            if (col_scale) {
+              v = __fmul_rn(v, col_scale[c]);
+            }
+          }
+          split3f(v, t[0][j], t[1][j], t[2][j]);
         }
-        split3f(v, t[0], t[1], t[2]);
-      } else {
-        t[0] = t[1] = t[2] = __float2bfloat16(0.0f);
+        __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nstore * cpad + c0;
+        for (int k = 0; k < nstore; ++k) {
+          uint2 packed;
+          packed.x = static_cast<uint32_t>(__bfloat16_as_ushort(t[k][0])) |
+                     (static_cast<uint32_t>(__bfloat16_as_ushort(t[k][1])) << 16);
+          packed.y = static_cast<uint32_t>(__bfloat16_as_ushort(t[k][2])) |
+                     (static_cast<uint32_t>(__bfloat16_as_ushort(t[k][3])) << 16);
+          *reinterpret_cast<uint2*>(row + k * cpad) = packed;
+        }
       }
-      __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nstore * cpad;
-      for (int k = 0; k < nstore; ++k) {
-        row[k * cpad + c] = t[k];
-      }
+    }
+
+    dim3 split_grid(int rows, int cpad) {
+      return dim3(static_cast<unsigned>((cpad / 4 + 255) / 256), static_cast<unsigned>(std::min(rows, 65535)));
     }
 
     // Kernel matrix in FP64: K[e][g] = J_g F(e_b / e_peak(g)) with the plan's table,
@@ -739,9 +755,8 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
     return RG_OK;
   }
   auto          s  = static_cast<cudaStream_t>(stream);
-  const int64_t nA = static_cast<int64_t>(ndist) * pl->gpad;
-  rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
-    f, ndist, pl->ng, pl->ng, nullptr, pl->d_A, pl->gpad, pl->nstore);
+  rg::split_rows_kernel<<<rg::split_grid(ndist, pl->gpad), 256, 0, s>>>(f, ndist, pl->ng, pl->ng, nullptr,
+                                                                         pl->d_A, pl->gpad, pl->nstore);
   RG_CUDA_TRY(cudaGetLastError());
   rg::GemmArgs g {};
   g.M         = ndist;
@@ -763,9 +778,8 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
     return RG_OK;
   }
   auto          s  = static_cast<cudaStream_t>(stream);
-  const int64_t nA = static_cast<int64_t>(ndist) * pl->epad;
   // left operand: dL/dS[d][e] * e_e
-  rg::split_rows_kernel<<<static_cast<unsigned>((nA + 255) / 256), 256, 0, s>>>(
+  rg::split_rows_kernel<<<rg::split_grid(ndist, pl->epad), 256, 0, s>>>(
     grad_out, ndist, pl->nbins, pl->nbins, pl->d_ebins, pl->d_AT, pl->epad, pl->nstore);
   RG_CUDA_TRY(cudaGetLastError());
   rg::GemmArgs g {};

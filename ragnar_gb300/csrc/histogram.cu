@@ -135,7 +135,17 @@ namespace rg {
           const int   k = bin_of(U, p, thr);
           atomicAdd(&cnt[k], 1u);
           if (p.log_spaced) {
-            const float v = p.fourvel ? __frcp_rn(sqrtf(U)) : inv_sqrt_one_plus(U);
+            // 1/|u|: rsqrt and one Newton step (within an ulp; the reference rounds this
+            // value through double, so the sums are compared with a tolerance anyway)
+            float v;
+            if (!p.fourvel) {
+              v = inv_sqrt_one_plus(U);
+            } else if (U > 0.0f && U < 3.0e38f) {
+              const float r = rsqrtf(U);
+              v             = __fmul_rn(r, __fmaf_rn(__fmul_rn(-0.5f * U, r), r, 1.5f));
+            } else {
+              v = __frcp_rn(sqrtf(U)); // 0 -> inf, inf -> 0, NaN -> NaN
+            }
             atomicAdd(&sum32[k], v);
           }
         };
@@ -175,19 +185,35 @@ namespace rg {
       }
     }
 
-    __global__ void histogram_reduce_kernel(const unsigned long long* __restrict__ pc,
-                                            const double* __restrict__ ps, int grid, int nbins,
-                                            int log_spaced, float* __restrict__ hist,
-                                            unsigned long long* __restrict__ counts) {
-      const int k = blockIdx.x * blockDim.x + threadIdx.x;
-      if (k >= nbins) {
-        return;
-      }
+    // Block (32 bins x 32 row groups): row group y sums block partials y, y + 32, ...
+    // then the groups are combined in order (deterministic).
+    constexpr int kHistReduceRows = 32;
+
+    __global__ void __launch_bounds__(32 * kHistReduceRows)
+      histogram_reduce_kernel(const unsigned long long* __restrict__ pc, const double* __restrict__ ps,
+                              int grid, int nbins, int log_spaced, float* __restrict__ hist,
+                              unsigned long long* __restrict__ counts) {
+      __shared__ unsigned long long c_part[kHistReduceRows][33];
+      __shared__ double             s_part[kHistReduceRows][33];
+      const int k  = blockIdx.x * 32 + threadIdx.x;
+      const int ty = threadIdx.y;
       unsigned long long c = 0;
       double             s = 0.0;
-      for (int b = 0; b < grid; ++b) {
-        c += pc[static_cast<int64_t>(b) * nbins + k];
-        s += ps[static_cast<int64_t>(b) * nbins + k];
+      if (k < nbins) {
+        for (int b = ty; b < grid; b += kHistReduceRows) {
+          c += pc[static_cast<int64_t>(b) * nbins + k];
+          s += ps[static_cast<int64_t>(b) * nbins + k];
+        }
+      }
+      c_part[ty][threadIdx.x] = c;
+      s_part[ty][threadIdx.x] = s;
+      __syncthreads();
+      if (ty != 0 || k >= nbins) {
+        return;
+      }
+      for (int y = 1; y < kHistReduceRows; ++y) {
+        c += c_part[y][threadIdx.x];
+        s += s_part[y][threadIdx.x];
       }
       hist[k] = log_spaced ? __double2float_rn(s) : static_cast<float>(c);
       if (counts) {
@@ -355,7 +381,7 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
   p.part_sums   = reinterpret_cast<double*>(buf + off_ps);
   rg::histogram_kernel<<<G, rg::kHistThreads, smem, s>>>(p);
   RG_CUDA_TRY(cudaGetLastError());
-  rg::histogram_reduce_kernel<<<(nbins + 127) / 128, 128, 0, s>>>(
+  rg::histogram_reduce_kernel<<<(nbins + 31) / 32, dim3(32, rg::kHistReduceRows), 0, s>>>(
     p.part_counts, p.part_sums, G, nbins, p.log_spaced, hist,
     reinterpret_cast<unsigned long long*>(counts));
   RG_CUDA_TRY(cudaGetLastError());

@@ -1,0 +1,251 @@
+// Inverse-Compton spectrum on sm_103a: ICSpectrum (ic.cpp:15-46), ic::Kernel
+// (ic.hpp:67-94) and KNfunc (ic.hpp:20-25).
+//
+//   S[e] = sum_g sum_s f_g (f_s / e_s) e^2 KN(Gamma, q) / g^k      (k = 1 for log-spaced
+//          gamma bins, 2 for linear ones), over the (g, s) pairs with e <= g Gamma / (1 + Gamma),
+//   Gamma = 4 g e_s,  q = (e / g) / (Gamma (1 - e / g)),
+//   KN(Gamma, q) = 2 q ln q + (1 - q) (1 + 2 q + (Gamma q)^2 / (2 (1 + Gamma q))).
+//
+// Rewritten so that the per-(g, s, e) work is one multiply and one logarithm:
+//   t = Gamma q = e / (g - e) depends on (e, g) only; g - e is exact in FP32 where it
+//     matters (e in [g/2, g]), so t avoids the reference's 1 - e/g cancellation;
+//   q = t / Gamma = (t / g) (1 / (4 e_s));  e <= g Gamma / (1 + Gamma)  <=>  q <= 1 (e < g);
+//   KN = q (2 ln 2) log2 q + ((1 + h) + (1 - h) q - 2 q^2),  h = t^2 / (2 (1 + t)).
+// Per eval: FMUL (q), two FMNMX (clamp for the log), MUFU.LG2, FMUL + FFMA (log term), two FFMA
+// (quadratic), select of the weight, FFMA into the FP32 accumulator.
+//
+// Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
+// (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
+// e^2 f_g / g^k and folded into a double-float; per-warp FP64 partials are reduced in a
+// fixed order by a second kernel (deterministic).  Non-positive or non-finite IC bins give
+// 0 (the reference produces NaN there).
+#include "rg_common.cuh"
+#include "rg_internal.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace rg {
+
+  namespace {
+
+    constexpr int kIcThreads = 256;
+    constexpr int kIcWarps   = kIcThreads / 32;
+    constexpr int kIcSlice   = 512;
+    constexpr int kIcSChunk  = 64; // soft photons per work item
+
+    struct IcParams {
+      const float* gb;      // ng gamma (gamma beta) bins
+      const float* fp;      // ng particle distribution
+      int          ng;
+      int          log_spaced;
+      const float* inv4es;  // ns: 1 / (4 e_s)
+      const float* ws;      // ns: f_s / e_s
+      int          ns;
+      const float* eic;     // ne IC photon energies
+      int          ne;
+      int          nslices;
+      double*      partials; // [grid][nslices][kIcWarps][kIcSlice]
+    };
+
+    __global__ void ic_prep_kernel(const float* __restrict__ es, const float* __restrict__ fs, int ns,
+                                   float* __restrict__ inv4es, float* __restrict__ ws) {
+      const int s = blockIdx.x * blockDim.x + threadIdx.x;
+      if (s < ns) {
+        inv4es[s] = __frcp_rn(__fmul_rn(4.0f, es[s]));
+        ws[s]     = __fdiv_rn(fs[s], es[s]);
+      }
+    }
+
+    template <int K>
+    __global__ void __launch_bounds__(kIcThreads, 2) ic_kernel(const __grid_constant__ IcParams p) {
+      const int     lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      const int     slice = blockIdx.y;
+      const int     nsc   = (p.ns + kIcSChunk - 1) / kIcSChunk;
+      const int64_t items = static_cast<int64_t>(p.ng) * nsc;
+      const int64_t G = gridDim.x, b = blockIdx.x;
+      const int64_t i0 = b * items / G, i1 = (b + 1) * items / G;
+
+      // this lane's IC energy of row k (0 for padding and for invalid bins); reloaded
+      // where needed (per item) instead of held in registers
+      auto energy = [&](int k) -> float {
+        const int   bin = slice * kIcSlice + k * 32 + lane;
+        const float e   = bin < p.ne ? __ldg(p.eic + bin) : 0.0f;
+        return (e > 0.0f && isfinite(e)) ? e : 0.0f;
+      };
+      float hi[K], lo[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        hi[k] = 0.0f;
+        lo[k] = 0.0f;
+      }
+      const float two_ln2 = 1.3862943611198906f;
+
+      for (int64_t it = i0 + warp; it < i1; it += kIcWarps) {
+        const int   g     = static_cast<int>(it / nsc);
+        const int   s0    = static_cast<int>(it - static_cast<int64_t>(g) * nsc) * kIcSChunk;
+        const int   s1    = min(p.ns, s0 + kIcSChunk);
+        const float gv    = __ldg(p.gb + g);
+        const float fv    = __ldg(p.fp + g);
+        if (!(gv > 0.0f) || !isfinite(gv)) {
+          continue; // non-positive or non-finite gamma bins contribute nothing (warp-uniform)
+        }
+        const float inv_g = __frcp_rn(gv);
+        // per (e, g): t / g, 1 + h, 1 - h; q = (t / g) / (4 e_s) > 1 marks no contribution
+        float tg[K], A0[K], A1[K], acc[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float e = energy(k);
+          const float d = __fsub_rn(gv, e);
+          float       t = 0.0f, h = 0.0f;
+          if (e > 0.0f && d > 0.0f) {
+            t = __fdiv_rn(e, d);
+            h = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(t, t)), __fadd_rn(1.0f, t));
+          } else {
+            t = 3.0e38f; // q = huge: every soft photon fails q <= 1
+          }
+          tg[k]  = __fmul_rn(t, inv_g);
+          A0[k]  = __fadd_rn(1.0f, h);
+          A1[k]  = __fsub_rn(1.0f, h);
+          acc[k] = 0.0f;
+        }
+        for (int s = s0; s < s1; ++s) {
+          const float i4 = __ldg(p.inv4es + s);
+          const float w  = __ldg(p.ws + s);
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            const float q  = __fmul_rn(tg[k], i4);
+            // finite log argument: q > 1 is masked below; below 1e-30 the q ln q term is
+            // < 1e-28 and the clamp keeps log2 off denormals
+            const float qc = fminf(fmaxf(q, 1e-30f), 2.0f);
+            const float lq = __log2f(qc);
+            const float poly = __fmaf_rn(__fmaf_rn(-2.0f, qc, A1[k]), qc, A0[k]);
+            const float kn   = __fmaf_rn(__fmul_rn(qc, two_ln2), lq, poly);
+            acc[k]           = __fmaf_rn(q <= 1.0f ? w : 0.0f, kn, acc[k]);
+          }
+        }
+        // scale by e^2 f_g / g^k and fold into the double-float sums
+        const float fg = p.log_spaced ? __fmul_rn(fv, inv_g) : __fmul_rn(__fmul_rn(fv, inv_g), inv_g);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float e    = energy(k);
+          const float term = __fmul_rn(__fmul_rn(acc[k], fg), __fmul_rn(e, e));
+          const ff    sm   = two_sum(hi[k], term);
+          hi[k]            = sm.hi;
+          lo[k]            = __fadd_rn(lo[k], sm.lo);
+        }
+      }
+      double* dst = p.partials + ((b * p.nslices + slice) * kIcWarps + warp) * kIcSlice;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        dst[k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
+      }
+    }
+
+    // out[e] = sum over blocks and warps (fixed order) of the partials; 32 bins x 32 row groups.
+    __global__ void __launch_bounds__(1024)
+      ic_reduce_kernel(const double* __restrict__ partials, int grid, int nslices, int ne, float* __restrict__ out) {
+      __shared__ double part[32][33];
+      const int bin = blockIdx.x * 32 + threadIdx.x, ty = threadIdx.y;
+      double    sum = 0.0;
+      if (bin < ne) {
+        const int slice = bin / kIcSlice, j = bin % kIcSlice;
+        const int rows  = grid * kIcWarps;
+        for (int r = ty; r < rows; r += 32) {
+          const int blk = r / kIcWarps, w = r % kIcWarps;
+          sum += partials[((static_cast<int64_t>(blk) * nslices + slice) * kIcWarps + w) * kIcSlice + j];
+        }
+      }
+      part[ty][threadIdx.x] = sum;
+      __syncthreads();
+      if (ty == 0 && bin < ne) {
+        double t = 0.0;
+        for (int y = 0; y < 32; ++y) {
+          t += part[y][threadIdx.x];
+        }
+        out[bin] = __double2float_rn(t);
+      }
+    }
+
+    template <int K>
+    cudaError_t launch_ic_k(const IcParams& p, dim3 grid, cudaStream_t s) {
+      ic_kernel<K><<<grid, kIcThreads, 0, s>>>(p);
+      return cudaGetLastError();
+    }
+
+    cudaError_t launch_ic(int K, const IcParams& p, dim3 grid, cudaStream_t s) {
+      switch (K) {
+#define RG_IC_K(k)                                                                                   \
+  case k:                                                                                            \
+    return launch_ic_k<k>(p, grid, s);
+        RG_IC_K(1) RG_IC_K(2) RG_IC_K(3) RG_IC_K(4) RG_IC_K(5) RG_IC_K(6) RG_IC_K(7) RG_IC_K(8)
+        RG_IC_K(9) RG_IC_K(10) RG_IC_K(11) RG_IC_K(12) RG_IC_K(13) RG_IC_K(14) RG_IC_K(15) RG_IC_K(16)
+#undef RG_IC_K
+        default:
+          return cudaErrorInvalidValue;
+      }
+    }
+
+  } // namespace
+
+} // namespace rg
+
+extern "C" {
+
+int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_spaced, const float* es,
+                   const float* fs, int32_t ns, const float* eic, int32_t ne, float* out, void* stream) {
+  rg::clear_error();
+  if (ng < 0 || ns < 0 || ne < 0 || (ng > 0 && (!gbins || !f)) || (ns > 0 && (!es || !fs)) ||
+      (ne > 0 && (!eic || !out))) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_ic_spectrum: bad arguments");
+  }
+  auto s = static_cast<cudaStream_t>(stream);
+  if (ne == 0) {
+    return RG_OK;
+  }
+  if (ng == 0 || ns == 0) {
+    RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * ne, s));
+    return RG_OK;
+  }
+  rg::DeviceContext* ctx = nullptr;
+  RG_TRY(rg::context(&ctx));
+  const int     nslices = (ne + rg::kIcSlice - 1) / rg::kIcSlice;
+  const int     K       = std::min(16, (std::min(ne, rg::kIcSlice) + 31) / 32);
+  const int64_t items   = static_cast<int64_t>(ng) * ((ns + rg::kIcSChunk - 1) / rg::kIcSChunk);
+  const int     grid    = static_cast<int>(std::max<int64_t>(
+    1, std::min<int64_t>(2 * ctx->sms, (items + rg::kIcWarps - 1) / rg::kIcWarps)));
+  // one stream-ordered scratch allocation: inv4es, ws, partials
+  const size_t off_ws   = 256 * ((sizeof(float) * ns + 255) / 256);
+  const size_t off_part = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
+  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * rg::kIcWarps * rg::kIcSlice;
+  unsigned char* buf    = nullptr;
+  RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
+  rg::IcParams p {};
+  p.gb         = gbins;
+  p.fp         = f;
+  p.ng         = ng;
+  p.log_spaced = log_spaced ? 1 : 0;
+  p.inv4es     = reinterpret_cast<float*>(buf);
+  p.ws         = reinterpret_cast<float*>(buf + off_ws);
+  p.ns         = ns;
+  p.eic        = eic;
+  p.ne         = ne;
+  p.nslices    = nslices;
+  p.partials   = reinterpret_cast<double*>(buf + off_part);
+  rg::ic_prep_kernel<<<(ns + 255) / 256, 256, 0, s>>>(es, fs, ns, reinterpret_cast<float*>(buf),
+                                                       reinterpret_cast<float*>(buf + off_ws));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = rg::launch_ic(K, p, dim3(grid, nslices), s);
+  if (e == cudaSuccess) {
+    rg::ic_reduce_kernel<<<dim3((ne + 31) / 32), dim3(32, 32), 0, s>>>(p.partials, grid, nslices, ne, out);
+    e = cudaGetLastError();
+  }
+  const cudaError_t ef = cudaFreeAsync(buf, s);
+  if (e != cudaSuccess) {
+    return rg::cuda_error(e, "rg_ic_spectrum launch");
+  }
+  RG_CUDA_TRY(ef);
+  return RG_OK;
+}
+
+} // extern "C"

@@ -434,6 +434,36 @@ namespace rgh {
     return out;
   }
 
+  // ICSpectrum (ic.cpp:15-46) with the unit checks of ic::Kernel (ic.hpp:57-63).
+  Array1D<float> ic_spectrum(const TabulatedDistribution& dist_prtls, const TabulatedDistribution& dist_soft,
+                             const Bins& bins_e_ic) {
+    if (dist_soft.bins.unit != EnergyUnits::mec2) {
+      throw std::runtime_error("Soft photons energy bins must be in units of mec^2");
+    }
+    if (bins_e_ic.unit != EnergyUnits::mec2) {
+      throw std::runtime_error("E_ic must be in units of mec^2");
+    }
+    if (g_verbose) {
+      py::print("Computing IC spectrum ...", "flush"_a = true);
+      py::print(" Launching",
+                human(static_cast<double>(dist_prtls.f.extent()) * dist_soft.f.extent() * bins_e_ic.extent()),
+                "threads", "end"_a = "", "flush"_a = true);
+    }
+    Array1D<float> out(bins_e_ic.extent());
+    if (out.n > 0) {
+      py::gil_scoped_release nogil;
+      check(rg_ic_spectrum(dist_prtls.bins.data(), dist_prtls.f.data(), static_cast<int32_t>(dist_prtls.f.extent()),
+                           dist_prtls.bins.log_spaced ? 1 : 0, dist_soft.bins.data(), dist_soft.f.data(),
+                           static_cast<int32_t>(dist_soft.f.extent()), bins_e_ic.data(),
+                           static_cast<int32_t>(bins_e_ic.extent()), out.data(), nullptr));
+      check(rg_stream_synchronize(nullptr));
+    }
+    if (g_verbose) {
+      py::print(": OK", "flush"_a = true);
+    }
+    return out;
+  }
+
   float ffunc_integrand(float x) {
     Array1D<float> dx = Array1D<float>::from_host(&x, 1);
     Array1D<float> dy(1);
@@ -722,6 +752,8 @@ PYBIND11_MODULE(_ragnar, m) {
   define_particles<3>(m);
 
   m.def("Ffunc_integrand", &ffunc_integrand, "x"_a);
+  m.def("ICSpectrum", &ic_spectrum, "dist_prtls"_a, "dist_soft_photons"_a, "bins_e_ic"_a,
+        "Compute the IC spectrum E^2 dN/dE of a particle distribution on a soft-photon distribution");
   m.def("SynchrotronSpectrumFromDist", &synchrotron_spectrum_from_dist, "dist_prtls"_a,
         "bins_e_syn"_a, "g_syn"_a, "e_syn_at_g_syn"_a,
         "Compute the synchrotron spectrum E^2 dN/dE from a distribution of particles");

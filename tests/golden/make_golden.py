@@ -7,6 +7,7 @@ API returns for seeded inputs.  Run from the repository root where the
 reference tree is present:
 
     bash oracle/build_ref.sh && OMP_NUM_THREADS=8 python tests/golden/make_golden.py
+    OMP_NUM_THREADS=8 python tests/golden/make_golden.py ic     # ic.npz only
 
 The fixtures are small (.npz, a few hundred KB in total) and are committed; the
 tests never need the reference tree.
@@ -149,5 +150,31 @@ def main() -> None:
     print("golden fixtures written to", HERE)
 
 
+def make_ic(rg) -> None:
+    """ICSpectrum (ic.cpp:15-46): the reference test's configuration (tests/ic.py), a
+    steeper power law against a broader soft-photon field, and linear particle bins."""
+    ic = {}
+    cases = [("log", 1.5, 1e-8, 0.1), ("log", 2.5, 3e-9, 0.5), ("lin", 1.5, 1e-8, 0.1)]
+    for i, (kind, p, e_break, width) in enumerate(cases):
+        gb = rg.Logbins(1e3, 1e7, 200) if kind == "log" else rg.Linbins(1e3, 1e7, 200)
+        dist_prtls = rg.TabulatedDistribution(gb, rg.PlawGenerator(-p, 1e3, 1e7))
+        dist_soft = rg.TabulatedDistribution(rg.Logbins(1e-11, 1e-7, 200, rg.EnergyUnits.mec2),
+                                             rg.DeltaGenerator(e_break, e_break * width))
+        bins_eic = rg.Bins(rg.Logspace(1e3, 1e7, 200), rg.EnergyUnits.mec2)
+        ic[f"case{i}_gb"] = dist_prtls.EnergyBins().as_array()
+        ic[f"case{i}_f"] = dist_prtls.F().as_array()
+        ic[f"case{i}_log"] = np.array(kind == "log")
+        ic[f"case{i}_es"] = dist_soft.EnergyBins().as_array()
+        ic[f"case{i}_fs"] = dist_soft.F().as_array()
+        ic[f"case{i}_eic"] = bins_eic.as_array()
+        ic[f"case{i}_ref"] = rg.ICSpectrum(dist_prtls, dist_soft, bins_eic).as_array()
+    np.savez_compressed(os.path.join(HERE, "ic.npz"), **ic)
+    print("ic.npz written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["ic"]:
+        make_ic(load_reference())
+    else:
+        main()
+        make_ic(load_reference())

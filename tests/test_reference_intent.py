@@ -52,3 +52,15 @@ def test_isotropic_helper_is_unit_norm():
     rng = np.random.default_rng(0)
     v = isotropic(rng, 1000, np.ones(1000))
     assert np.allclose(np.sqrt(v[0] ** 2 + v[1] ** 2 + v[2] ** 2), 1.0, atol=1e-6)
+
+
+def test_ic_slope_and_peak(oracle_lib):
+    """The reference's own IC checks (tests/ic.py:15-54), on its configuration: for a
+    particle power law of index -p the Thomson-regime slope of E^2 dN/dE is -p/2 + 3/2
+    (to 1e-2 between 2e3 and 2e4), and the peak sits at e_break * gamma_max^2 (10 %)."""
+    g = golden("ic")
+    args = (g["case0_gb"], g["case0_f"], True, g["case0_es"], g["case0_fs"], g["case0_eic"])
+    x = g["case0_eic"].astype(np.float64)
+    y = oracle_lib.ic_spectrum_f64(*args)
+    assert abs(slope(x, y, 2e3, 2e4) - (-1.5 / 2 + 1.5)) < 1e-2
+    assert abs(x[np.argmax(y)] / (1e-8 * 1e7**2) - 1.0) < 0.1
