@@ -57,11 +57,12 @@ def parse_args():
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm", "histogram"],
+    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm", "histogram", "ic"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
                          "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
-                         "energyDistribution of 3.3e7 particles into 200 log bins, 4 calls")
+                         "energyDistribution of 3.3e7 particles into 200 log bins, 4 calls; 'ic' = "
+                         "ICSpectrum 1024 x 1024 x 1024, 4 calls")
     return ap.parse_args()
 
 
@@ -860,6 +861,14 @@ def main():
         return
     if args.profile_case == "histogram":
         profile_histogram_case()
+        return
+    if args.profile_case == "ic":
+        import torch  # noqa: PLC0415
+
+        from ragnar_gb300 import capi  # noqa: PLC0415
+
+        capi.check(capi.lib().rg_init(0))
+        print(json.dumps(ic_case(torch, capi, torch.device("cuda", 0))))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

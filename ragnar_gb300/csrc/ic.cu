@@ -11,8 +11,8 @@
 //     matters (e in [g/2, g]), so t avoids the reference's 1 - e/g cancellation;
 //   q = t / Gamma = (t / g) (1 / (4 e_s));  e <= g Gamma / (1 + Gamma)  <=>  q <= 1 (e < g);
 //   KN = q (2 ln 2) log2 q + ((1 + h) + (1 - h) q - 2 q^2),  h = t^2 / (2 (1 + t)).
-// Per eval: FMUL (q), two FMNMX (clamp for the log), MUFU.LG2, FMUL + FFMA (log term), two FFMA
-// (quadratic), select of the weight, FFMA into the FP32 accumulator.
+// Per eval: FMUL (q), FMNMX (lower clamp for the log), MUFU.LG2, FMUL + FFMA (log term), two
+// FFMA (quadratic), select of KN (q <= 1), FFMA into the FP32 accumulator.
 //
 // Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
 // (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
@@ -115,13 +115,13 @@ namespace rg {
 #pragma unroll
           for (int k = 0; k < K; ++k) {
             const float q  = __fmul_rn(tg[k], i4);
-            // finite log argument: q > 1 is masked below; below 1e-30 the q ln q term is
-            // < 1e-28 and the clamp keeps log2 off denormals
-            const float qc = fminf(fmaxf(q, 1e-30f), 2.0f);
-            const float lq = __log2f(qc);
+            // below 1e-30 the q ln q term is < 1e-28 and the clamp keeps log2 off
+            // denormals; q > 1 (or NaN) selects 0 whatever KN evaluated to
+            const float qc   = fmaxf(q, 1e-30f);
+            const float lq   = lg2_normal(qc); // qc >= 1e-30 is a normal float
             const float poly = __fmaf_rn(__fmaf_rn(-2.0f, qc, A1[k]), qc, A0[k]);
             const float kn   = __fmaf_rn(__fmul_rn(qc, two_ln2), lq, poly);
-            acc[k]           = __fmaf_rn(q <= 1.0f ? w : 0.0f, kn, acc[k]);
+            acc[k]           = __fmaf_rn(w, q <= 1.0f ? kn : 0.0f, acc[k]);
           }
         }
         // scale by e^2 f_g / g^k and fold into the double-float sums

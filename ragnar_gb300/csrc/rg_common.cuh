@@ -76,6 +76,14 @@ namespace rg {
     return false;
   }
 
+  // Hardware base-2 logarithm (PTX lg2.approx.ftz.f32) for arguments known to be
+  // normal floats: no denormal-input handling around the MUFU operation.
+  __device__ __forceinline__ float lg2_normal(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+  }
+
   // ---- error-free transformations (double-float arithmetic) ----------------
 
   struct ff {

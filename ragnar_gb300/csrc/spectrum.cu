@@ -1018,9 +1018,9 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
   const float* host[rg::kComps];
   rg::particle_comps(p, host);
   RG_CUDA_TRY(cudaMemsetAsync(pl->d_acc64, 0, sizeof(double) * pl->nbins, s));
-  // staging may still be read by earlier work on `s`
-  RG_CUDA_TRY(cudaEventRecord(pl->consumed[0], s));
-  RG_CUDA_TRY(cudaEventRecord(pl->consumed[1], s));
+  // consumed[b] was last recorded after the kernel that read staging buffer b (by an
+  // earlier call of this plan, or never): the first copies of this call wait for
+  // exactly that, so they overlap the tail of the previous call's kernels
   const int64_t n = p->n;
   for (int64_t c = 0, a = 0; a < n; ++c, a += kStageChunk) {
     const int     b = static_cast<int>(c & 1);
