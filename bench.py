@@ -717,6 +717,40 @@ def adam_fit_case(torch, capi, device, steps=200):
     torch.cuda.synchronize()
     t_step = a.elapsed_time(b) / 1e3 / (steps - 1)
     l1 = float(loss.detach())
+
+    # the same step captured once into a CUDA graph (forward GEMM, loss, transpose-GEMM
+    # backward, Adam update) and replayed: no per-op launch or Python overhead
+    theta_g = (-2.0 * lg).float().repeat(nd, 1).contiguous().requires_grad_(True)
+    opt_g = torch.optim.Adam([theta_g], lr=0.05, capturable=True)
+
+    def step_g():
+        loss = loss_of(rt.synchrotron_from_dist_batched(plan, torch.exp(theta_g)))
+        loss.backward()
+        opt_g.step()
+        return loss
+
+    side = torch.cuda.Stream(device)
+    side.wait_stream(torch.cuda.current_stream(device))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            opt_g.zero_grad(set_to_none=True)
+            step_g()
+    torch.cuda.current_stream(device).wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    opt_g.zero_grad(set_to_none=True)
+    with torch.cuda.graph(graph):
+        loss_static = step_g()
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps - 1):
+        graph.replay()
+    b.record()
+    torch.cuda.synchronize()
+    t_graph = a.elapsed_time(b) / 1e3 / (steps - 1)
+    l_graph = float(loss_static.detach())
+
     # final forward and gradient against FP64
     f = torch.exp(theta.detach()).contiguous().requires_grad_(True)
     S = rt.synchrotron_from_dist_batched(plan, f)
@@ -735,6 +769,7 @@ def adam_fit_case(torch, capi, device, steps=200):
     plan.close()
     return {"distributions": nd, "gamma_bins": ng, "photon_bins": ne, "adam_steps": steps,
             "ms_per_adam_step": t_step * 1e3, "gemm_evals_per_s": 2.0 * nd * ng * ne / t_step,
+            "ms_per_adam_step_cuda_graph": t_graph * 1e3, "loss_after_graphed_steps": l_graph,
             "loss_first": l0, "loss_last": l1,
             "fwd_max_rel_err_vs_fp64": float(np.max(np.abs(Sg[mm] - S64[mm]) / S64[mm])),
             "grad_max_err_vs_fp64_rel_to_row_max": float(np.max(np.abs(gg - g64) /

@@ -194,3 +194,31 @@ def test_every_tile_shape(gpu, oracle_lib, table, cfg):
     assert np.max(np.abs(gf.cpu().numpy() - want) / np.max(np.abs(want), axis=1, keepdims=True)) < 1e-5
     with pytest.raises(capi.RgError, match="out of range"):
         plan.set_config(3, 0)
+
+
+def test_forward_and_adjoint_replay_from_cuda_graph(gpu, oracle_lib):
+    """The split + GEMM forward and the transpose-GEMM adjoint make no host
+    synchronisation or allocation, so a training step can be captured once and replayed."""
+    gb = oracle_lib.logspace(1.0, 1e5, 200)
+    bins = oracle_lib.logspace(0.01, 1e11, 256)
+    plan = rt.fromdist_plan(gb, bins, max_dist=64)
+    f = torch.from_numpy(_dists(gb, 64, seed=31)).to(gpu)
+    w = torch.rand((64, 256), device=gpu)
+    S = torch.empty((64, 256), device=gpu)
+    gf = torch.empty((64, 200), device=gpu)
+    stream = torch.cuda.current_stream(gpu).cuda_stream
+    plan.run(f, S, stream)  # warm (configures the kernels) outside the capture
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        s = torch.cuda.current_stream(gpu).cuda_stream
+        plan.run(f, S, s)
+        plan.adjoint(w, gf, s)
+    f.mul_(2.0)  # replays read the inputs as they are at replay time
+    graph.replay()
+    plan.check()
+    S_ref = torch.empty_like(S)
+    gf_ref = torch.empty_like(gf)
+    plan.run(f, S_ref)
+    plan.adjoint(w, gf_ref)
+    plan.check()
+    assert torch.equal(S, S_ref) and torch.equal(gf, gf_ref)
