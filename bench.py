@@ -57,7 +57,7 @@ def parse_args():
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "gemm", "histogram", "ic"],
+    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "spectrum200", "gemm", "histogram", "ic"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
                          "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
@@ -849,6 +849,31 @@ def profile_case():
     print("profile case done")
 
 
+def profile_case_200():
+    """4 launches of the fused kernel on 2^22 particles of the 1e6-particle configuration's
+    kind (|u| ~ u^-2 on [1, 100], isotropic, B = z, w = 1) x 200 bins 0.01..1e7."""
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    n = 1 << 22
+    gen = torch.Generator(device=device).manual_seed(5)
+    u = config1_particles(torch, n, gen, device)
+    prt = capi.particles(u, b=[None, None, torch.ones(n, device=device)], n=n)
+    plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 200), 1.0, 1.0, 1.0)
+    out = torch.empty(200, device=device)
+    flush = torch.empty(64 << 20, device=device)
+    for _ in range(4):
+        flush.fill_(1.0)
+        plan.run(prt, out, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    plan.check()
+    plan.close()
+    print("profile case (200 bins) done")
+
+
 def profile_gemm_case():
     """4 launches of the split + tcgen05 GEMM forward on 4096 x 1024 x 1024 (6 products)."""
     import numpy as np  # noqa: PLC0415
@@ -890,6 +915,9 @@ def main():
     args = parse_args()
     if args.profile_case == "spectrum":
         profile_case()
+        return
+    if args.profile_case == "spectrum200":
+        profile_case_200()
         return
     if args.profile_case == "gemm":
         profile_gemm_case()
