@@ -245,8 +245,8 @@ namespace rg {
       tc_fence_after();
       if (done && nk > 0) {
         const int row = m0 + warp * 32 + lane;
-#pragma unroll 1
         const bool two = nk > g.kpt; // accumulator 1 was written
+#pragma unroll 1
         for (int c = 0; c < kBN / 32; ++c) {
           float v[32];
           const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;

@@ -214,7 +214,6 @@ int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, in
   fp.htable      = nullptr;
   fp.hseg        = 0;
   fp.frac        = kFrac;
-  fp.tau_scale   = static_cast<float>(std::ldexp(1.0, -kFrac));
   fp.partials    = reinterpret_cast<double*>(b + kOffPartials);
   fp.nslices     = 1;
   fp.status      = reinterpret_cast<unsigned*>(b + kOffStatus);

@@ -41,7 +41,6 @@ namespace rg {
   // valid entry (T >> kFrac < 1024).
   constexpr int      kFrac        = 22;
   constexpr int      kRefEntries  = 1024;
-  constexpr uint32_t kFracMask    = (1u << kFrac) - 1u;
   // c1 is stored pre-multiplied by 2^127: a denormal built from the fraction
   // bits (bits * 2^-149) times c1 * 2^127 equals frac * c1.
   constexpr double   kSlopeScale  = 1.7014118346046923e38; // 2^127

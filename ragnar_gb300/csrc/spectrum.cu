@@ -722,7 +722,6 @@ namespace rg {
     fp.htable      = pl->smooth ? pl->smooth->d_coef : nullptr;
     fp.hseg        = kSmoothSegments;
     fp.frac        = pl->frac;
-    fp.tau_scale   = static_cast<float>(std::ldexp(1.0, -pl->frac));
     fp.partials    = pl->d_partials;
     fp.nslices     = pl->nslices;
     fp.status      = pl->d_status;

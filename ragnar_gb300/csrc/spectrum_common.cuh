@@ -53,7 +53,6 @@ namespace rg {
     const float4*  htable;
     int            hseg;
     int            frac;
-    float          tau_scale;    // 2^-frac
     double*        partials;     // [(grid + nseg) * nslices * kWarps * kSliceBins]
     int            nslices;
     unsigned*      status;
