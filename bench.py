@@ -646,10 +646,10 @@ def fromdist_gemm_case(torch, capi, device, peak_bf16):
         plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=nd, split_products=terms)
         tuned = plan.config()
         shapes = {}
-        for cfg, (bn, stages) in enumerate([(256, 4), (128, 6), (128, 3)]):
+        for cfg, (bn, stages) in enumerate([(256, 4), (128, 6), (128, 4)]):
             plan.set_config(cfg, -1)
             shapes[f"128x{bn}_s{stages}_ms"] = timed(torch, lambda: plan.run(f, out, stream), 10) * 1e3
-        plan.set_config([(256, 4), (128, 6), (128, 3)].index(tuned["fwd"]), -1)
+        plan.set_config([(256, 4), (128, 6), (128, 4)].index(tuned["fwd"]), -1)
         t = timed(torch, lambda: plan.run(f, out, stream), 20)
         plan.check(stream)
         K = plan.kernel_matrix()

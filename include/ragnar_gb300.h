@@ -280,7 +280,7 @@ int rg_fromdist_plan_config(const rg_fromdist_plan* plan, int32_t* fwd_bn, int32
                             int32_t* adj_bn, int32_t* adj_stages);
 
 /* Overrides the tuned shapes with entries 0..2 of the supported list
- * ((256, 4), (128, 6), (128, 3)); -1 keeps the current choice. */
+ * ((256, 4), (128, 6), (128, 4)); -1 keeps the current choice. */
 int rg_fromdist_plan_set_config(rg_fromdist_plan* plan, int32_t fwd_cfg, int32_t adj_cfg);
 
 /* Copies the FP64 kernel matrix K (nbins x ng) to host memory. */

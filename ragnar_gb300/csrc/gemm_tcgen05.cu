@@ -7,11 +7,8 @@
 // many distributions f[d, g] give one GEMM:  S[d, e] = e * sum_g f[d, g] K[e, g].
 //
 // Precision: FP32 operands are split into BF16 terms (x = h + m + l, each the
-// BF16 rounding of the remainder; for FP32 input every step is exact in FP32)
-// stored side by side, [h | m | l] per row, and the products are summed in one
-// GEMM whose k loop walks (product, gamma block) pairs -- the TMA producer maps
-// product t to the stored terms it multiplies -- accumulated in FP32 in tensor
-// memory:
+// BF16 rounding of the remainder; for FP32 input every step is exact in FP32) and
+// the products are summed in one GEMM, accumulated in FP32 in tensor memory:
 //   6 products  (h.h + h.m + m.h + h.l + l.h + m.m): ~1e-8 relative per product (default)
 //   3 products  (h.h + h.m + m.h):                  ~1e-5 relative per product (fast)
 // The dominant h.h product accumulates in its own TMEM accumulator and the
@@ -20,14 +17,19 @@
 // the large running sum bounds the accumulation error by the h.h steps alone
 // (4 per 64 gamma bins) instead of by all of them.
 //
-// GEMM: C[M x N] = A[M x K'] . B[N x K']^T, both operands K-major BF16.  CTA tile
-// 128 x 256, K step 64; TMA (cp.async.bulk.tensor, 128-byte swizzle) fills a
-// 4-stage shared-memory ring; one thread issues tcgen05.mma (M 128, N 256, K 16)
-// into one of two 128 x 256 FP32 accumulators in tensor memory and commits
-// each stage back to the producer; after the last commit all four warps read
-// both accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and
-// write (acc0 + acc1) * col_scale.  Every mbarrier wait is bounded; a wait that gives up records
-// the status word, and the CTA still frees its tensor memory.
+// GEMM: C[M x N] = A[M x K] . B[N x K]^T.  The right operand (the kernel matrix,
+// split once per plan) is stored as BF16 terms [h | m | l] per row and streamed
+// by TMA (cp.async.bulk.tensor, 128-byte swizzle) through a ring of k blocks.  The
+// left operand (the distributions, FP32) is read by eight converter warps, split
+// exactly into its BF16 terms and written straight into 128-byte-swizzled shared
+// tiles, double-buffered per 64-gamma block: no split kernel and no BF16 copy in
+// HBM.  The k loop runs gamma block outer, product inner, so each converted tile
+// serves every product that uses it.  One thread issues tcgen05.mma (M 128, N =
+// tile width, K 16) and commits each ring stage back to the producer and each
+// left buffer back to the converters; after the last commit warps 0..3 read both
+// accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
+// (acc0 + acc1) * col_scale.  Every mbarrier wait is bounded; a wait that gives up
+// records the status word, and the CTA still frees its tensor memory.
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
 
@@ -49,15 +51,14 @@ namespace rg {
     constexpr int kBM       = 128;
     constexpr int kBK       = 64; // bf16 elements = 128 bytes: one swizzle row
     constexpr int kUmmaK    = 16;
-    constexpr int kGemmThreads = 128;
-    constexpr uint32_t kBytesA = kBM * kBK * 2;
+    constexpr int kGemmThreads = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 convert the left operand
 
     // Tile shapes the autotuner chooses from: N width of the CTA tile (M is 128)
     // and the depth of the TMA ring.  Two FP32 accumulators of `bn` TMEM columns.
     struct GemmConfig {
       int bn, stages;
     };
-    constexpr GemmConfig kConfigs[] = { { 256, 4 }, { 128, 6 }, { 128, 3 } };
+    constexpr GemmConfig kConfigs[] = { { 256, 4 }, { 128, 6 }, { 128, 4 } };
     constexpr int        kNumConfigs = 3;
     constexpr unsigned kDevGemmTimeout = 8u;
     // products h.h, h.m, m.h, h.l, l.h, m.m: stored term (0 h, 1 m, 2 l) of each operand
@@ -136,40 +137,75 @@ namespace rg {
       }
     }
 
+    // Splits v into BF16 terms h, m, l (each the rounding of the remainder).
+    __device__ __forceinline__ void split3(double v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+      h         = __double2bfloat16(v);
+      double r  = v - static_cast<double>(__bfloat162float(h));
+      m         = __double2bfloat16(r);
+      r        -= static_cast<double>(__bfloat162float(m));
+      l         = __double2bfloat16(r);
+    }
+
+    // The same for an FP32 value: h is within a binade of v, so v - h and the next
+    // remainder are exact in FP32 (at most 17 significant bits).
+    __device__ __forceinline__ void split3f(float v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+      h       = __float2bfloat16_rn(v);
+      float r = __fsub_rn(v, __bfloat162float(h));
+      m       = __float2bfloat16_rn(r);
+      r       = __fsub_rn(r, __bfloat162float(m));
+      l       = __float2bfloat16_rn(r);
+    }
+
+    __device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
+      return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
+    }
+
     struct GemmArgs {
       int          M, N;
-      int          kpt;      // k blocks per product (padded K / kBK)
-      int          nprod;    // products: 6 or 3 (the first is h.h, accumulator 0)
+      int          kpt;        // k blocks of 64 (padded K / kBK)
+      int          nprod;      // products: 6 or 3 (the first is h.h, accumulator 0)
+      int          nstore;     // BF16 terms of each operand: 3 (h, m, l) or 2 (h, m)
+      const float* left;       // M x cols FP32 left operand, row stride ld
+      int          cols, ld;
+      const float* left_scale; // per left column (nullable)
       float*       C;
       int          ldc;
-      const float* col_scale; // nullable
+      const float* col_scale;  // per output column (nullable)
       unsigned*    status;
     };
 
+    // Warps 2..9 turn the FP32 left operand into BF16 terms in shared memory.
+    constexpr int      kConvWarps  = 8;
+    constexpr int      kConvThreads = 32 * kConvWarps;
+    constexpr uint32_t kBytesTerm  = kBM * kBK * 2; // one 128 x 64 BF16 term tile (16 KB)
+
     template <int kBN, int kStages>
     __global__ void __launch_bounds__(kGemmThreads, 1)
-      gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                          const __grid_constant__ GemmArgs g) {
+      gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmB, const __grid_constant__ GemmArgs g) {
       constexpr uint32_t kBytesB   = kBN * kBK * 2;
       constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
       constexpr uint32_t kIdesc    = idesc<kBN>();
       extern __shared__ __align__(1024) unsigned char smem_raw[];
-      // 1024-byte alignment of the swizzled stage buffers
+      // 1024-byte alignment of the swizzled tiles
       unsigned char* smem = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-      unsigned char* sA = smem;
-      unsigned char* sB = smem + kStages * kBytesA;
-      __shared__ uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
+      unsigned char* sB = smem;                      // kStages right-operand tiles (TMA)
+      unsigned char* sA = smem + kStages * kBytesB;  // 2 buffers x nstore left-operand term tiles
+      __shared__ uint64_t b_full[kStages], b_empty[kStages], a_full[2], a_empty[2], done_bar;
       __shared__ uint32_t tmem_slot;
 
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
-      const int nk = g.nprod * g.kpt;
+      const int nk = g.nprod * g.kpt; // k loop: gamma block outer, product inner
 
       if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
-          mbar_init(&full_bar[s], 1);
-          mbar_init(&empty_bar[s], 1);
+          mbar_init(&b_full[s], 1);
+          mbar_init(&b_empty[s], 1);
+        }
+        for (int s = 0; s < 2; ++s) {
+          mbar_init(&a_full[s], kConvWarps);
+          mbar_init(&a_empty[s], 1);
         }
         mbar_init(&done_bar, 1);
         fence_mbar_init();
@@ -186,52 +222,126 @@ namespace rg {
       tc_fence_after();
       const uint32_t tmem_d = tmem_slot;
 
-      int issued = 0; // k blocks the producer handed to TMA
+      int issued = 0; // right-operand k blocks handed to TMA
       if (warp == 0 && lane == 0) {
-        // ---- producer: TMA into the ring --------------------------------------------
+        // ---- producer: TMA of the right operand into the ring ---------------------------
         for (int kb = 0; kb < nk; ++kb, ++issued) {
           const int      s  = kb % kStages;
           const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
-          if (kb >= kStages && !mbar_wait_bounded(&empty_bar[s], ph ^ 1u)) {
+          if (kb >= kStages && !mbar_wait_bounded(&b_empty[s], ph ^ 1u)) {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
-          // product t = kb / kpt multiplies stored term kLeft[t] of A by kRight[t] of B
-          const int t = kb / g.kpt, gblk = kb - t * g.kpt;
-          mbar_arrive_expect_tx(&full_bar[s], kBytesA + kBytesB);
-          tma_load_2d(sA + s * kBytesA, &tmA, (kLeft[t] * g.kpt + gblk) * kBK, m0, &full_bar[s]);
-          tma_load_2d(sB + s * kBytesB, &tmB, (kRight[t] * g.kpt + gblk) * kBK, n0, &full_bar[s]);
+          // product t multiplies left term kLeft[t] by right term kRight[t] of gamma block gb
+          const int gb = kb / g.nprod, t = kb - gb * g.nprod;
+          mbar_arrive_expect_tx(&b_full[s], kBytesB);
+          tma_load_2d(sB + s * kBytesB, &tmB, (kRight[t] * g.kpt + gb) * kBK, n0, &b_full[s]);
         }
       } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer ----------------------------------------------------------------
-        bool ok = true;
+        // ---- MMA issuer -------------------------------------------------------------------
+        bool     ok      = true;
         uint32_t started = 0; // bit a: accumulator a holds a partial sum
-        for (int kb = 0; kb < nk && ok; ++kb) {
-          const int      s  = kb % kStages;
-          const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
-          if (!mbar_wait_bounded(&full_bar[s], ph)) {
+        for (int gb = 0; gb < g.kpt && ok; ++gb) {
+          const int ab = gb & 1;
+          if (!mbar_wait_bounded(&a_full[ab], static_cast<uint32_t>(gb >> 1) & 1u)) {
             atomicOr(g.status, kDevGemmTimeout);
-            ok = false;
             break;
           }
-          tc_fence_after();
-          const uint64_t da = smem_desc_sw128(sA + s * kBytesA);
-          const uint64_t db = smem_desc_sw128(sB + s * kBytesB);
-          const uint32_t acc = kb < g.kpt ? 0u : 1u;
+          for (int t = 0; t < g.nprod; ++t) {
+            const int      kb = gb * g.nprod + t;
+            const int      s  = kb % kStages;
+            const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
+            if (!mbar_wait_bounded(&b_full[s], ph)) {
+              atomicOr(g.status, kDevGemmTimeout);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t da  = smem_desc_sw128(sA + (ab * g.nstore + kLeft[t]) * kBytesTerm);
+            const uint64_t db  = smem_desc_sw128(sB + s * kBytesB);
+            const uint32_t acc = t == 0 ? 0u : 1u;
 #pragma unroll
-          for (int k = 0; k < kBK / kUmmaK; ++k) {
-            // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
-            mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k), kIdesc,
-                     ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
+            for (int k = 0; k < kBK / kUmmaK; ++k) {
+              // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
+              mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k), kIdesc,
+                       ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
+            }
+            started |= 1u << acc;
+            mma_commit(&b_empty[s]);
           }
-          started |= 1u << acc;
-          mma_commit(&empty_bar[s]);
+          mma_commit(&a_empty[ab]); // the left tiles of gamma block gb are free once these MMAs complete
         }
         mma_commit(&done_bar);
+      } else if (warp >= 2) {
+        // ---- converters: FP32 left operand -> BF16 terms, 128-byte swizzled -----------------
+        const int  ct  = threadIdx.x - 64;
+        const bool vec = (g.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(g.left) & 15) == 0;
+        for (int gb = 0; gb < g.kpt; ++gb) {
+          const int ab = gb & 1;
+          if (gb >= 2 &&
+              !__all_sync(0xffffffffu, mbar_wait_bounded(&a_empty[ab], static_cast<uint32_t>((gb - 2) >> 1) & 1u))) {
+            if (lane == 0) {
+              atomicOr(g.status, kDevGemmTimeout);
+            }
+            break;
+          }
+          unsigned char* tile = sA + ab * g.nstore * kBytesTerm;
+          // unit = 8 consecutive k of one row (a 16-byte chunk of each term tile); all of
+          // this thread's loads are issued before any is used, to keep them in flight together
+          constexpr int kUnits = (kBM * kBK / 8) / kConvThreads;
+          float         v[kUnits][8];
+#pragma unroll
+          for (int i = 0; i < kUnits; ++i) {
+            const int    u = ct + kConvThreads * i;
+            const int    row = m0 + (u >> 3), k0 = gb * kBK + (u & 7) * 8;
+            const float* src = g.left + static_cast<int64_t>(row) * g.ld + k0;
+            if (row < g.M && vec && k0 + 8 <= g.cols) {
+              const float4 p0 = __ldg(reinterpret_cast<const float4*>(src));
+              const float4 p1 = __ldg(reinterpret_cast<const float4*>(src) + 1);
+              v[i][0] = p0.x; v[i][1] = p0.y; v[i][2] = p0.z; v[i][3] = p0.w;
+              v[i][4] = p1.x; v[i][5] = p1.y; v[i][6] = p1.z; v[i][7] = p1.w;
+            } else {
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                v[i][j] = (row < g.M && k0 + j < g.cols) ? __ldg(src + j) : 0.0f;
+              }
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < kUnits; ++i) {
+            const int u = ct + kConvThreads * i;
+            const int r = u >> 3, c = u & 7, k0 = gb * kBK + c * 8;
+            __nv_bfloat16 h[8], m[8], l[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              float x = v[i][j];
+              if (g.left_scale && k0 + j < g.cols) {
+                x = __fmul_rn(x, __ldg(g.left_scale + k0 + j));
+              }
+              split3f(x, h[j], m[j], l[j]);
+            }
+            // 128-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ (r % 8)
+            const uint32_t off = static_cast<uint32_t>((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+            *reinterpret_cast<uint4*>(tile + off) =
+              make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
+            *reinterpret_cast<uint4*>(tile + kBytesTerm + off) =
+              make_uint4(pack_bf16x2(m[0], m[1]), pack_bf16x2(m[2], m[3]), pack_bf16x2(m[4], m[5]), pack_bf16x2(m[6], m[7]));
+            if (g.nstore > 2) {
+              *reinterpret_cast<uint4*>(tile + 2 * kBytesTerm + off) =
+                make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+            }
+          }
+          // generic-proxy stores -> visible to the tensor core's async-proxy reads
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(&a_full[ab]);
+          }
+        }
       }
       __syncwarp();
 
-      // ---- epilogue: TMEM -> registers -> global ---------------------------------------
+      // ---- epilogue: TMEM -> registers -> global (warps 0..3 own TMEM lanes 0..127) -----------
       // tcgen05.ld is warp-collective: every thread takes the same branch
       const bool done = __syncthreads_and(mbar_wait_bounded(&done_bar, 0)) != 0;
       if (!done && threadIdx.x == 0) {
@@ -239,16 +349,16 @@ namespace rg {
         // a wait gave up: let the copies still in flight land before the CTA exits
         for (int s = 0; s < kStages && s < issued; ++s) {
           const int last = s + ((issued - 1 - s) / kStages) * kStages;
-          mbar_wait_bounded(&full_bar[s], static_cast<uint32_t>(last / kStages) & 1u);
+          mbar_wait_bounded(&b_full[s], static_cast<uint32_t>(last / kStages) & 1u);
         }
       }
       tc_fence_after();
-      if (done && nk > 0) {
-        const int row = m0 + warp * 32 + lane;
-        const bool two = nk > g.kpt; // accumulator 1 was written
+      if (done && nk > 0 && warp < 4) {
+        const int  row = m0 + warp * 32 + lane;
+        const bool two = g.nprod > 1; // accumulator 1 was written
 #pragma unroll 1
         for (int c = 0; c < kBN / 32; ++c) {
-          float v[32];
+          float          v[32];
           const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
           tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
           if (two) {
@@ -293,67 +403,6 @@ namespace rg {
     }
 
     // ---- operand preparation -------------------------------------------------------------
-
-    // Splits v into BF16 terms h, m, l (each the rounding of the remainder).
-    __device__ __forceinline__ void split3(double v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
-      h         = __double2bfloat16(v);
-      double r  = v - static_cast<double>(__bfloat162float(h));
-      m         = __double2bfloat16(r);
-      r        -= static_cast<double>(__bfloat162float(m));
-      l         = __double2bfloat16(r);
-    }
-
-    // The same for an FP32 value: h is within a binade of v, so v - h and the next
-    // remainder are exact in FP32 (at most 17 significant bits).
-    __device__ __forceinline__ void split3f(float v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
-      h       = __float2bfloat16_rn(v);
-      float r = __fsub_rn(v, __bfloat162float(h));
-      m       = __float2bfloat16_rn(r);
-      r       = __fsub_rn(r, __bfloat162float(m));
-      l       = __float2bfloat16_rn(r);
-    }
-
-    // dst[r][t * cpad + c] = term t (h, m, l; the first nstore) of src[r][c] * scale[c]
-    // (zero in the padding), FP32 throughout.  Thread = 4 consecutive columns of one
-    // row (cpad is a multiple of 64, so every 4-column group is inside the row and
-    // each term's 4 BF16 values are one aligned 8-byte store); rows stride by gridDim.y.
-    __global__ void split_rows_kernel(const float* __restrict__ src, int rows, int cols, int ld,
-                                      const float* __restrict__ col_scale, __nv_bfloat16* __restrict__ dst,
-                                      int cpad, int nstore) {
-      const int c0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-      if (c0 >= cpad) {
-        return;
-      }
-      for (int r = blockIdx.y; r < rows; r += gridDim.y) {
-        const float* srow = src + static_cast<int64_t>(r) * ld;
-        __nv_bfloat16 t[3][4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int c = c0 + j;
-          float     v = 0.0f;
-          if (c < cols) {
-            v = srow[c];
-            if (col_scale) {
-              v = __fmul_rn(v, col_scale[c]);
-            }
-          }
-          split3f(v, t[0][j], t[1][j], t[2][j]);
-        }
-        __nv_bfloat16* row = dst + static_cast<int64_t>(r) * nstore * cpad + c0;
-        for (int k = 0; k < nstore; ++k) {
-          uint2 packed;
-          packed.x = static_cast<uint32_t>(__bfloat16_as_ushort(t[k][0])) |
-                     (static_cast<uint32_t>(__bfloat16_as_ushort(t[k][1])) << 16);
-          packed.y = static_cast<uint32_t>(__bfloat16_as_ushort(t[k][2])) |
-                     (static_cast<uint32_t>(__bfloat16_as_ushort(t[k][3])) << 16);
-          *reinterpret_cast<uint2*>(row + k * cpad) = packed;
-        }
-      }
-    }
-
-    dim3 split_grid(int rows, int cpad) {
-      return dim3(static_cast<unsigned>((cpad / 4 + 255) / 256), static_cast<unsigned>(std::min(rows, 65535)));
-    }
 
     // Kernel matrix in FP64: K[e][g] = J_g F(e_b / e_peak(g)) with the plan's table,
     // written as the right operand (rows e) and its transpose (rows g).
@@ -447,37 +496,39 @@ namespace rg {
       return RG_OK;
     }
 
-    size_t gemm_smem(int cfg) {
-      return static_cast<size_t>(kConfigs[cfg].stages) * (kBytesA + kConfigs[cfg].bn * kBK * 2) + 1024;
+    // right-operand ring + two buffers of the left operand's BF16 term tiles + alignment slack
+    size_t gemm_smem(int cfg, int nstore) {
+      return static_cast<size_t>(kConfigs[cfg].stages) * kConfigs[cfg].bn * kBK * 2 +
+             static_cast<size_t>(2 * nstore) * kBytesTerm + 1024;
     }
 
     template <int BN, int STAGES>
-    int launch_gemm_t(int cfg, const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+    int launch_gemm_t(int cfg, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
       static bool configured = false;
       if (!configured) {
         RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, STAGES>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(gemm_smem(cfg))));
+                                         static_cast<int>(gemm_smem(cfg, 3))));
         configured = true;
       }
       const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM);
-      gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg), s>>>(tA, tB, g);
+      gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg, g.nstore), s>>>(tB, g);
       RG_CUDA_TRY(cudaGetLastError());
       return RG_OK;
     }
 
     // tB is the right operand's tensor map whose box height is the config's bn.
-    int launch_gemm(int cfg, const CUtensorMap& tA, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+    int launch_gemm(int cfg, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
       if (g.M <= 0 || g.N <= 0) {
         return RG_OK;
       }
       switch (cfg) {
         case 0:
-          return launch_gemm_t<kConfigs[0].bn, kConfigs[0].stages>(0, tA, tB, g, s);
+          return launch_gemm_t<kConfigs[0].bn, kConfigs[0].stages>(0, tB, g, s);
         case 1:
-          return launch_gemm_t<kConfigs[1].bn, kConfigs[1].stages>(1, tA, tB, g, s);
+          return launch_gemm_t<kConfigs[1].bn, kConfigs[1].stages>(1, tB, g, s);
         case 2:
-          return launch_gemm_t<kConfigs[2].bn, kConfigs[2].stages>(2, tA, tB, g, s);
+          return launch_gemm_t<kConfigs[2].bn, kConfigs[2].stages>(2, tB, g, s);
         default:
           return set_error(RG_ERR_ARGUMENT, "unknown GEMM configuration");
       }
@@ -504,13 +555,11 @@ struct rg_fromdist_plan {
   float*         d_gbeta = nullptr;
   float*         d_ebins = nullptr; // photon energies with invalid bins set to 0
   double*        d_K     = nullptr; // nbins x ng kernel matrix (FP64)
-  // BF16 terms [h | m | l] (the first nstore) per row
+  // right operands as BF16 terms [h | m | l] (the first nstore) per row; the left operand
+  // (distributions, or dL/dS) is split inside the GEMM
   __nv_bfloat16* d_B     = nullptr; // forward right operand  [nbins x nstore*gpad]
   __nv_bfloat16* d_BT    = nullptr; // adjoint right operand  [ng x nstore*epad]
-  __nv_bfloat16* d_A     = nullptr; // forward left operand   [max_dist x nstore*gpad]
-  __nv_bfloat16* d_AT    = nullptr; // adjoint left operand   [max_dist x nstore*epad]
   unsigned*      d_status = nullptr;
-  CUtensorMap    tA, tAT;
   CUtensorMap    tB[2], tBT[2]; // right operands with box height 256 and 128
   int            cfg_fwd = 0, cfg_adj = 0; // autotuned tile shapes
 };
@@ -531,6 +580,10 @@ namespace rg {
       g.N         = adjoint ? pl->ng : pl->nbins;
       g.kpt       = (adjoint ? pl->epad : pl->gpad) / kBK;
       g.nprod     = pl->nprod;
+      g.nstore    = pl->nstore;
+      g.cols      = adjoint ? pl->nbins : pl->ng;
+      g.ld        = g.cols;
+      g.left_scale = adjoint ? pl->d_ebins : nullptr;
       g.ldc       = g.N;
       g.col_scale = adjoint ? nullptr : pl->d_ebins;
       g.status    = pl->d_status;
@@ -544,9 +597,11 @@ namespace rg {
         }
       }
       float*      C  = nullptr;
+      float*      L  = nullptr; // zero left operand for the timing runs
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       auto cleanup = [&]() {
         cudaFree(C);
+        cudaFree(L);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
       };
@@ -557,27 +612,27 @@ namespace rg {
       cudaError_t e = cudaMalloc(&C, sizeof(float) * static_cast<size_t>(g.M) * g.N);
       if (e == cudaSuccess) e = cudaEventCreate(&e0);
       if (e == cudaSuccess) e = cudaEventCreate(&e1);
-      const size_t abytes = sizeof(__nv_bfloat16) * static_cast<size_t>(pl->max_dist) * pl->nstore *
-                            (adjoint ? pl->epad : pl->gpad);
-      if (e == cudaSuccess) e = cudaMemset(adjoint ? pl->d_AT : pl->d_A, 0, abytes);
+      const size_t lbytes = sizeof(float) * static_cast<size_t>(g.M) * g.cols;
+      if (e == cudaSuccess) e = cudaMalloc(&L, lbytes);
+      if (e == cudaSuccess) e = cudaMemset(L, 0, lbytes);
       if (e != cudaSuccess) {
         return fail(cuda_error(e, "GEMM autotuning setup"));
       }
       g.C        = C;
+      g.left     = L;
       int   best = 0;
       float best_ms = 0.0f;
       for (int cfg = 0; cfg < kNumConfigs; ++cfg) {
-        const CUtensorMap& tA = adjoint ? pl->tAT : pl->tA;
         const CUtensorMap& tB = adjoint ? pl->tBT[box_index(cfg)] : pl->tB[box_index(cfg)];
         for (int r = 0; r < 2; ++r) {
-          const int st = launch_gemm(cfg, tA, tB, g, nullptr);
+          const int st = launch_gemm(cfg, tB, g, nullptr);
           if (st != RG_OK) {
             return fail(st);
           }
         }
         e = cudaEventRecord(e0, nullptr);
         for (int r = 0; r < 5 && e == cudaSuccess; ++r) {
-          const int st = launch_gemm(cfg, tA, tB, g, nullptr);
+          const int st = launch_gemm(cfg, tB, g, nullptr);
           if (st != RG_OK) {
             return fail(st);
           }
@@ -673,8 +728,6 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
   RG_PLAN_CUDA(cudaMalloc(&pl->d_K, sizeof(double) * nbins * ng));
   RG_PLAN_CUDA(cudaMalloc(&pl->d_B, sizeof(__nv_bfloat16) * nbins * kf));
   RG_PLAN_CUDA(cudaMalloc(&pl->d_BT, sizeof(__nv_bfloat16) * ng * ka));
-  RG_PLAN_CUDA(cudaMalloc(&pl->d_A, sizeof(__nv_bfloat16) * max_dist * kf));
-  RG_PLAN_CUDA(cudaMalloc(&pl->d_AT, sizeof(__nv_bfloat16) * max_dist * ka));
   RG_PLAN_CUDA(cudaMalloc(&pl->d_status, sizeof(unsigned)));
   RG_PLAN_CUDA(cudaMemset(pl->d_status, 0, sizeof(unsigned)));
   RG_PLAN_CUDA(cudaMemcpy(pl->d_gbeta, gbeta, sizeof(float) * ng, cudaMemcpyHostToDevice));
@@ -714,8 +767,7 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
                                                                             pl->epad, pl->nstore);
   RG_PLAN_CUDA(cudaGetLastError());
   RG_PLAN_CUDA(cudaDeviceSynchronize());
-  int st = rg::encode_tiled(&pl->tA, pl->d_A, kf, max_dist, rg::kBM);
-  if (st == RG_OK) st = rg::encode_tiled(&pl->tAT, pl->d_AT, ka, max_dist, rg::kBM);
+  int st = RG_OK;
   for (int b = 0; b < 2 && st == RG_OK; ++b) {
     const uint32_t box = b == 0 ? 256u : 128u;
     st = rg::encode_tiled(&pl->tB[b], pl->d_B, kf, nbins, box);
@@ -740,8 +792,6 @@ int rg_fromdist_plan_destroy(rg_fromdist_plan* pl) {
   cudaFree(pl->d_K);
   cudaFree(pl->d_B);
   cudaFree(pl->d_BT);
-  cudaFree(pl->d_A);
-  cudaFree(pl->d_AT);
   cudaFree(pl->d_status);
   delete pl;
   return RG_OK;
@@ -754,20 +804,21 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
   if (ndist == 0) {
     return RG_OK;
   }
-  auto          s  = static_cast<cudaStream_t>(stream);
-  rg::split_rows_kernel<<<rg::split_grid(ndist, pl->gpad), 256, 0, s>>>(f, ndist, pl->ng, pl->ng, nullptr,
-                                                                         pl->d_A, pl->gpad, pl->nstore);
-  RG_CUDA_TRY(cudaGetLastError());
   rg::GemmArgs g {};
-  g.M         = ndist;
-  g.N         = pl->nbins;
-  g.kpt       = pl->gpad / rg::kBK;
-  g.nprod     = pl->nprod;
-  g.C         = out;
-  g.ldc       = pl->nbins;
-  g.col_scale = pl->d_ebins;
-  g.status    = pl->d_status;
-  return rg::launch_gemm(pl->cfg_fwd, pl->tA, pl->tB[rg::box_index(pl->cfg_fwd)], g, s);
+  g.M          = ndist;
+  g.N          = pl->nbins;
+  g.kpt        = pl->gpad / rg::kBK;
+  g.nprod      = pl->nprod;
+  g.nstore     = pl->nstore;
+  g.left       = f;
+  g.cols       = pl->ng;
+  g.ld         = pl->ng;
+  g.left_scale = nullptr;
+  g.C          = out;
+  g.ldc        = pl->nbins;
+  g.col_scale  = pl->d_ebins;
+  g.status     = pl->d_status;
+  return rg::launch_gemm(pl->cfg_fwd, pl->tB[rg::box_index(pl->cfg_fwd)], g, static_cast<cudaStream_t>(stream));
 }
 
 int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndist, float* grad_f, void* stream) {
@@ -777,21 +828,22 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
   if (ndist == 0) {
     return RG_OK;
   }
-  auto          s  = static_cast<cudaStream_t>(stream);
-  // left operand: dL/dS[d][e] * e_e
-  rg::split_rows_kernel<<<rg::split_grid(ndist, pl->epad), 256, 0, s>>>(
-    grad_out, ndist, pl->nbins, pl->nbins, pl->d_ebins, pl->d_AT, pl->epad, pl->nstore);
-  RG_CUDA_TRY(cudaGetLastError());
+  // left operand: dL/dS[d][e] * e_e (scaled while it is split)
   rg::GemmArgs g {};
-  g.M         = ndist;
-  g.N         = pl->ng;
-  g.kpt       = pl->epad / rg::kBK;
-  g.nprod     = pl->nprod;
-  g.C         = grad_f;
-  g.ldc       = pl->ng;
-  g.col_scale = nullptr;
-  g.status    = pl->d_status;
-  return rg::launch_gemm(pl->cfg_adj, pl->tAT, pl->tBT[rg::box_index(pl->cfg_adj)], g, s);
+  g.M          = ndist;
+  g.N          = pl->ng;
+  g.kpt        = pl->epad / rg::kBK;
+  g.nprod      = pl->nprod;
+  g.nstore     = pl->nstore;
+  g.left       = grad_out;
+  g.cols       = pl->nbins;
+  g.ld         = pl->nbins;
+  g.left_scale = pl->d_ebins;
+  g.C          = grad_f;
+  g.ldc        = pl->ng;
+  g.col_scale  = nullptr;
+  g.status     = pl->d_status;
+  return rg::launch_gemm(pl->cfg_adj, pl->tBT[rg::box_index(pl->cfg_adj)], g, static_cast<cudaStream_t>(stream));
 }
 
 int rg_fromdist_plan_check(rg_fromdist_plan* pl, void* stream) {

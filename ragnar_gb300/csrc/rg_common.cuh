@@ -43,6 +43,10 @@ namespace rg {
       : "memory");
   }
 
+  __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+  }
+
   // 1-D bulk copy global -> shared, completion signalled on `bar` (transaction
   // bytes).  dst, src and bytes must be multiples of 16.
   __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,

@@ -181,7 +181,8 @@ def test_every_tile_shape(gpu, oracle_lib, table, cfg):
     f = _dists(gb, 200, seed=40 + cfg)
     plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=200)
     tuned = plan.config()
-    assert tuned["fwd"] in [(256, 4), (128, 6), (128, 3)] and tuned["adj"] in [(256, 4), (128, 6), (128, 3)]
+    shapes = [(256, 4), (128, 6), (128, 4)]
+    assert tuned["fwd"] in shapes and tuned["adj"] in shapes
     plan.set_config(cfg, cfg)
     S = _run(plan, f, gpu)
     S64 = oracle_lib.sync_from_dist_f64(gb, f, True, bins, 1.0, 1.0, table)
