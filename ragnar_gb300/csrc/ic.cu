@@ -11,8 +11,9 @@
 //     matters (e in [g/2, g]), so t avoids the reference's 1 - e/g cancellation;
 //   q = t / Gamma = (t / g) (1 / (4 e_s));  e <= g Gamma / (1 + Gamma)  <=>  q <= 1 (e < g);
 //   KN = q (2 ln 2) log2 q + ((1 + h) + (1 - h) q - 2 q^2),  h = t^2 / (2 (1 + t)).
-// Per eval: FMUL (q), FMNMX (lower clamp for the log), MUFU.LG2, FMUL + FFMA (log term), two
-// FFMA (quadratic), select of KN (q <= 1), FFMA into the FP32 accumulator.
+// Per eval: FMUL (q), MUFU.LG2, FMUL + FFMA (log term), two FFMA (quadratic), select of KN
+// (q <= 1), FFMA into the FP32 accumulator.  q >= 1e-30 is guaranteed by a floor on t/g set
+// per (e, g) from the smallest 1 / (4 e_s), so the log's argument is always a normal float.
 //
 // Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
 // (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
@@ -40,6 +41,7 @@ namespace rg {
       int          ng;
       int          log_spaced;
       const float* inv4es;  // ns: 1 / (4 e_s)
+      const float* inv4es_min; // min over s of 1 / (4 e_s) (positive values), one float
       const float* ws;      // ns: f_s / e_s
       int          ns;
       const float* eic;     // ne IC photon energies
@@ -48,12 +50,20 @@ namespace rg {
       double*      partials; // [grid][nslices][kIcWarps][kIcSlice]
     };
 
+    // inv4es, ws and the smallest positive inv4es (positive floats order like their bit
+    // patterns, so an unsigned atomicMin finds it; the slot starts at +inf)
     __global__ void ic_prep_kernel(const float* __restrict__ es, const float* __restrict__ fs, int ns,
-                                   float* __restrict__ inv4es, float* __restrict__ ws) {
+                                   float* __restrict__ inv4es, float* __restrict__ ws, unsigned* min_bits) {
       const int s = blockIdx.x * blockDim.x + threadIdx.x;
       if (s < ns) {
-        inv4es[s] = __frcp_rn(__fmul_rn(4.0f, es[s]));
-        ws[s]     = __fdiv_rn(fs[s], es[s]);
+        const float e  = es[s];
+        const bool  ok = e > 0.0f && isfinite(e); // non-positive soft-photon bins contribute nothing
+        const float i4 = ok ? __frcp_rn(__fmul_rn(4.0f, e)) : __int_as_float(0x7f800000); // q = inf: masked
+        inv4es[s]      = i4;
+        ws[s]          = ok ? __fdiv_rn(fs[s], e) : 0.0f;
+        if (ok && i4 > 0.0f) {
+          atomicMin(min_bits, __float_as_uint(i4));
+        }
       }
     }
 
@@ -80,6 +90,9 @@ namespace rg {
         lo[k] = 0.0f;
       }
       const float two_ln2 = 1.3862943611198906f;
+      // t/g >= this keeps q = (t/g) / (4 e_s) >= 1e-30 for every soft photon with e_s > 0:
+      // the log's argument stays a normal float without a per-eval clamp
+      const float tg_floor = __fdiv_rn(1e-30f, *p.inv4es_min);
 
       for (int64_t it = i0 + warp; it < i1; it += kIcWarps) {
         const int   g     = static_cast<int>(it / nsc);
@@ -104,7 +117,7 @@ namespace rg {
           } else {
             t = 3.0e38f; // q = huge: every soft photon fails q <= 1
           }
-          tg[k]  = __fmul_rn(t, inv_g);
+          tg[k]  = fmaxf(__fmul_rn(t, inv_g), tg_floor);
           A0[k]  = __fadd_rn(1.0f, h);
           A1[k]  = __fsub_rn(1.0f, h);
           acc[k] = 0.0f;
@@ -115,12 +128,11 @@ namespace rg {
 #pragma unroll
           for (int k = 0; k < K; ++k) {
             const float q  = __fmul_rn(tg[k], i4);
-            // below 1e-30 the q ln q term is < 1e-28 and the clamp keeps log2 off
-            // denormals; q > 1 (or NaN) selects 0 whatever KN evaluated to
-            const float qc   = fmaxf(q, 1e-30f);
-            const float lq   = lg2_normal(qc); // qc >= 1e-30 is a normal float
-            const float poly = __fmaf_rn(__fmaf_rn(-2.0f, qc, A1[k]), qc, A0[k]);
-            const float kn   = __fmaf_rn(__fmul_rn(qc, two_ln2), lq, poly);
+            // q >= 1e-30 by the floor on t/g (q ln q < 1e-28 below it), so the log's argument
+            // is a normal float; q > 1 (or NaN) selects 0 whatever KN evaluated to
+            const float lq   = lg2_normal(q);
+            const float poly = __fmaf_rn(__fmaf_rn(-2.0f, q, A1[k]), q, A0[k]);
+            const float kn   = __fmaf_rn(__fmul_rn(q, two_ln2), lq, poly);
             acc[k]           = __fmaf_rn(w, q <= 1.0f ? kn : 0.0f, acc[k]);
           }
         }
@@ -216,7 +228,8 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
     1, std::min<int64_t>(2 * ctx->sms, (items + rg::kIcWarps - 1) / rg::kIcWarps)));
   // one stream-ordered scratch allocation: inv4es, ws, partials
   const size_t off_ws   = 256 * ((sizeof(float) * ns + 255) / 256);
-  const size_t off_part = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
+  const size_t off_min  = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
+  const size_t off_part = off_min + 256;
   const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * rg::kIcWarps * rg::kIcSlice;
   unsigned char* buf    = nullptr;
   RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
@@ -232,9 +245,15 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   p.ne         = ne;
   p.nslices    = nslices;
   p.partials   = reinterpret_cast<double*>(buf + off_part);
-  rg::ic_prep_kernel<<<(ns + 255) / 256, 256, 0, s>>>(es, fs, ns, reinterpret_cast<float*>(buf),
-                                                       reinterpret_cast<float*>(buf + off_ws));
-  cudaError_t e = cudaGetLastError();
+  p.inv4es_min = reinterpret_cast<float*>(buf + off_min);
+  // the minimum slot starts at 0x7f7f7f7f (3.4e38, above any 1 / (4 e_s) of a positive float)
+  cudaError_t e = cudaMemsetAsync(buf + off_min, 0x7f, sizeof(unsigned), s);
+  if (e == cudaSuccess) {
+    rg::ic_prep_kernel<<<(ns + 255) / 256, 256, 0, s>>>(es, fs, ns, reinterpret_cast<float*>(buf),
+                                                         reinterpret_cast<float*>(buf + off_ws),
+                                                         reinterpret_cast<unsigned*>(buf + off_min));
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = rg::launch_ic(K, p, dim3(grid, nslices), s);
   if (e == cudaSuccess) {
     rg::ic_reduce_kernel<<<dim3((ne + 31) / 32), dim3(32, 32), 0, s>>>(p.partials, grid, nslices, ne, out);
