@@ -883,10 +883,11 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_partials);
   cudaFree(pl->d_prefix);
   cudaFree(pl->d_plain_acc);
-  cudaFree(pl->d_stage[0]);
-  cudaFree(pl->d_stage[1]);
+  for (float* b : pl->d_stage) {
+    cudaFree(b);
+  }
   cudaFree(pl->d_acc64);
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < rg_spectrum_plan::kStageBuffers; ++b) {
     if (pl->copied[b]) {
       cudaEventDestroy(pl->copied[b]);
     }
@@ -1003,9 +1004,13 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
     return RG_OK;
   }
   auto              s           = static_cast<cudaStream_t>(stream);
-  constexpr int64_t kStageChunk = int64_t(1) << 22; // particles per staged chunk
+  // 2^22-particle chunks, double-buffered (each chunk costs a kernel tail and a reduction,
+  // so chunks are kept large; 2^21-particle chunks and a third buffer were measured slower
+  // or no faster)
+  constexpr int64_t kStageChunk = int64_t(1) << 22;
+  constexpr int     kBuffers    = rg_spectrum_plan::kStageBuffers;
   if (!pl->d_stage[0]) {
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kBuffers; ++b) {
       RG_CUDA_TRY(cudaMalloc(&pl->d_stage[b], sizeof(float) * rg::kComps * kStageChunk));
       RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->copied[b], cudaEventDisableTiming));
       RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->consumed[b], cudaEventDisableTiming));
@@ -1022,7 +1027,7 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
   // exactly that, so they overlap the tail of the previous call's kernels
   const int64_t n = p->n;
   for (int64_t c = 0, a = 0; a < n; ++c, a += kStageChunk) {
-    const int     b = static_cast<int>(c & 1);
+    const int     b = static_cast<int>(c % kBuffers);
     const int64_t m = std::min(kStageChunk, n - a);
     RG_CUDA_TRY(cudaStreamWaitEvent(pl->copy_stream, pl->consumed[b], 0));
     const float* dev[rg::kComps] = {};

@@ -44,11 +44,13 @@ struct rg_spectrum_plan {
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
   // host-resident streaming: device staging for two chunks, a copy stream
-  float*       d_stage[2]  = { nullptr, nullptr };
+  // host-streaming staging: kStageBuffers device buffers of stage_chunk particles (all components)
+  static constexpr int kStageBuffers = 2;
+  float*       d_stage[kStageBuffers]  = {};
   int64_t      stage_chunk = 0;
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t  copied[2]   = { nullptr, nullptr };
-  cudaEvent_t  consumed[2] = { nullptr, nullptr };
+  cudaEvent_t  copied[kStageBuffers]   = {};
+  cudaEvent_t  consumed[kStageBuffers] = {};
   double*      d_acc64     = nullptr;
 };
 
