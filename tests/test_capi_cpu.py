@@ -110,7 +110,7 @@ REFERENCE_NAMES = [
     "PlawGenerator", "BrokenPlawGenerator", "DeltaGenerator", "TabulatedDistribution",
     "Particles_1D", "Particles_2D", "Particles_3D", "SynchrotronSpectrum_1D",
     "SynchrotronSpectrum_2D", "SynchrotronSpectrum_3D", "SynchrotronSpectrumFromDist",
-    "Ffunc_integrand",
+    "Ffunc_integrand", "ICSpectrum",
 ]
 
 
