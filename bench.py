@@ -57,7 +57,7 @@ def parse_args():
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "spectrum200", "gemm", "histogram", "ic"],
+    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "spectrum200", "smooth", "gemm", "histogram", "ic"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
                          "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
@@ -874,6 +874,35 @@ def profile_case_200():
     print("profile case (200 bins) done")
 
 
+def profile_case_smooth():
+    """The differentiable path on 2^22 particles (|u| ~ u^-2 on [1, 100], isotropic, B = z,
+    w = 1) x 512 bins 0.01..1e7 with the smooth table: 4 forward and 4 adjoint launches."""
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    n = 1 << 22
+    gen = torch.Generator(device=device).manual_seed(5)
+    u = config1_particles(torch, n, gen, device)
+    w = torch.ones(n, device=device)
+    prt = capi.particles(u, b=[None, None, torch.ones(n, device=device)], w=w, n=n)
+    plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 512), 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
+    out = torch.empty(512, device=device)
+    gS = torch.rand(512, device=device, generator=gen)
+    gw = torch.empty(n, device=device)
+    gu = [torch.empty(n, device=device) for _ in range(3)]
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(4):
+        plan.run(prt, out, stream)
+        plan.adjoint(prt, gS, gw, gu, stream)
+    torch.cuda.synchronize()
+    plan.check()
+    plan.close()
+    print("profile case (smooth table) done")
+
+
 def profile_gemm_case():
     """4 launches of the split + tcgen05 GEMM forward on 4096 x 1024 x 1024 (6 products)."""
     import numpy as np  # noqa: PLC0415
@@ -918,6 +947,9 @@ def main():
         return
     if args.profile_case == "spectrum200":
         profile_case_200()
+        return
+    if args.profile_case == "smooth":
+        profile_case_smooth()
         return
     if args.profile_case == "gemm":
         profile_gemm_case()
