@@ -185,7 +185,7 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
  * allocate device memory once they run (a process that hands its whole device
  * memory budget out at start-up, or a plugin inside one).  No counterpart in the
  * reference.  Same arguments and result (reference table); every byte of scratch
- * comes from one fixed file-scope device array of about 10.6 MB that each GPU
+ * comes from one fixed file-scope device array of about 1.4 MB that each GPU
  * loading the library keeps until exit, and the call makes no cudaMalloc,
  * cudaFree or other allocating call.  At most 512 photon bins (larger counts are
  * rejected with RG_ERR_ARGUMENT).  The first call on a device looks up the

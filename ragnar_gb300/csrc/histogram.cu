@@ -200,6 +200,8 @@ namespace rg {
       unsigned long long c = 0;
       double             s = 0.0;
       if (k < nbins) {
+        // unrolled so that several rows' loads are in flight (the adds stay in row order)
+#pragma unroll 8
         for (int b = ty; b < grid; b += kHistReduceRows) {
           c += pc[static_cast<int64_t>(b) * nbins + k];
           s += ps[static_cast<int64_t>(b) * nbins + k];

@@ -163,6 +163,8 @@ namespace rg {
       if (bin < ne) {
         const int slice = bin / kIcSlice, j = bin % kIcSlice;
         const int rows  = grid * kIcWarps;
+        // unrolled so that several rows' loads are in flight (the adds stay in row order)
+#pragma unroll 8
         for (int r = ty; r < rows; r += 32) {
           const int blk = r / kIcWarps, w = r % kIcWarps;
           sum += partials[((static_cast<int64_t>(blk) * nslices + slice) * kIcWarps + w) * kIcSlice + j];

@@ -12,7 +12,7 @@
 //
 // Limits and sharing:
 //  * at most kNoAllocMaxBins (512) photon bins, reference table only; the
-//    array is kNoAllocBytes (about 10.6 MB) and every GPU that loads the
+//    array is kNoAllocBytes (about 1.4 MB) and every GPU that loads the
 //    library holds it until the process exits;
 //  * the first call on a device (with that device current) looks up the
 //    array's device address with cudaGetSymbolAddress and builds the F table
@@ -59,7 +59,7 @@ namespace rg {
     constexpr size_t kOffGrids    = align256(kOffCoef + sizeof(float2) * kRefEntries);
     constexpr size_t kOffPartials = align256(kOffGrids + sizeof(float) * kTableNodes * 100);
     constexpr size_t kNoAllocBytes =
-      kOffPartials + sizeof(double) * static_cast<size_t>(kNoAllocMaxGrid) * kWarps * kSliceBins;
+      kOffPartials + sizeof(double) * static_cast<size_t>(kNoAllocMaxGrid) * kSliceBins;
 
   } // namespace
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -32,6 +33,9 @@ namespace rg {
       return rg_s_;                                                                     \
     }                                                                                   \
   } while (0)
+
+  // Particle streams of a spectrum input: u0 u1 u2 e0 e1 e2 b0 b1 b2 w.
+  constexpr int kComps = 10;
 
   // ---- F tables ---------------------------------------------------------------
 
@@ -65,16 +69,34 @@ namespace rg {
     double  ln_xmin = 0, dln = 0;
   };
 
+  // Device staging for host-resident particle streams.  Every host-input call on a
+  // device, whatever its plan, streams through the same buffers and copy stream, so
+  // consecutive calls form one pipeline: the first copies of a call overlap the last
+  // kernels of the previous one, and two plans never compete for the host link.
+  struct HostStaging {
+    static constexpr int     kBuffers = 2;
+    static constexpr int64_t kChunk   = int64_t(1) << 22; // particles per buffer (all components)
+    std::mutex   mu;                                       // held while a call enqueues its chunks
+    float*       d_stage[kBuffers]  = {};
+    cudaEvent_t  copied[kBuffers]   = {};
+    cudaEvent_t  consumed[kBuffers] = {};
+    cudaStream_t copy_stream        = nullptr;
+    uint64_t     issued             = 0; // chunks issued so far; chunk c uses buffer c % kBuffers
+  };
+
   struct DeviceContext {
     int         device = -1;
     int         sms    = 0;
     RefTable    ref;
     SmoothTable smooth;
     bool        ref_ready = false, smooth_ready = false;
+    std::unique_ptr<HostStaging> staging;
   };
 
   // Context of the current device (created on first use; builds tables lazily).
   int context(DeviceContext** ctx);
+  // The current device's host staging (allocated on first use).
+  int host_staging(HostStaging** out);
   int reference_table(const RefTable** t);
   int smooth_table(const SmoothTable** t);
 
@@ -82,6 +104,7 @@ namespace rg {
   int build_reference_table(int n, float xmin, float xmax, RefTable& t, cudaStream_t s);
   int build_smooth_table(SmoothTable& t, cudaStream_t s);
   void free_tables(DeviceContext& c);
+  void free_staging(DeviceContext& c);
 
   // Host grids with the reference's float/double arithmetic.
   float logspace_point(float start, float stop, std::size_t num, std::size_t i);

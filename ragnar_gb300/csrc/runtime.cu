@@ -79,6 +79,46 @@ namespace rg {
     return RG_OK;
   }
 
+  int host_staging(HostStaging** out) {
+    DeviceContext* c = nullptr;
+    RG_TRY(context(&c));
+    std::lock_guard<std::mutex> lock(ctx_mutex());
+    if (!c->staging) {
+      auto st = std::make_unique<HostStaging>();
+      for (int b = 0; b < HostStaging::kBuffers; ++b) {
+        RG_CUDA_TRY(cudaMalloc(&st->d_stage[b], sizeof(float) * kComps * HostStaging::kChunk));
+        RG_CUDA_TRY(cudaEventCreateWithFlags(&st->copied[b], cudaEventDisableTiming));
+        RG_CUDA_TRY(cudaEventCreateWithFlags(&st->consumed[b], cudaEventDisableTiming));
+      }
+      RG_CUDA_TRY(cudaStreamCreateWithFlags(&st->copy_stream, cudaStreamNonBlocking));
+      c->staging = std::move(st);
+    }
+    *out = c->staging.get();
+    return RG_OK;
+  }
+
+  void free_staging(DeviceContext& c) {
+    if (!c.staging) {
+      return;
+    }
+    HostStaging& st = *c.staging;
+    if (st.copy_stream) {
+      cudaStreamSynchronize(st.copy_stream);
+      cudaStreamDestroy(st.copy_stream);
+    }
+    for (int b = 0; b < HostStaging::kBuffers; ++b) {
+      if (st.consumed[b]) {
+        cudaEventSynchronize(st.consumed[b]);
+        cudaEventDestroy(st.consumed[b]);
+      }
+      if (st.copied[b]) {
+        cudaEventDestroy(st.copied[b]);
+      }
+      cudaFree(st.d_stage[b]);
+    }
+    c.staging.reset();
+  }
+
   void free_tables(DeviceContext& c) {
     cudaFree(c.ref.d_x);
     cudaFree(c.ref.d_y);
@@ -130,6 +170,7 @@ int rg_finalize(void) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(kv.first);
+    rg::free_staging(*kv.second);
     rg::free_tables(*kv.second);
     cudaSetDevice(cur);
   }

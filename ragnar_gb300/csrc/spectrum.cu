@@ -27,9 +27,10 @@
 //      staged), and three FFMAs evaluate the cubic.
 //  * Lanes own photon bins (32 consecutive bins per row, K rows per lane), warps
 //    own particles; per-warp FP32 register accumulators are folded into
-//    double-float accumulators after every chunk and flushed per warp to FP64
-//    scratch; a second kernel sums blocks and warps in FP64 in a fixed order, so
-//    results are bit-reproducible.
+//    double-float accumulators after every chunk; at a segment's end the block sums
+//    its warps in FP64 (warp order) into one partial row per block, and a second
+//    kernel sums the blocks' rows in FP64 in a fixed order, so results are
+//    bit-reproducible.
 //  * Particle streams (SoA FP32) are staged chunk by chunk into shared memory
 //    with 1-D TMA bulk copies (cp.async.bulk + mbarrier), double buffered.
 //  * Work items are (segment, chunk) pairs in particle order; each block of the
@@ -53,13 +54,44 @@ namespace rg {
 
   namespace {
 
+    // Rows of 32 bins combined per pass of flush_block: the pass's scratch, kFlushRows x
+    // kWarps x 32 doubles, is the 8 KB of the two (q, A) buffers.
+    constexpr int kFlushRows = 4;
+    static_assert(kFlushRows * kWarps * 32 * sizeof(double) <= 2 * kChunk * sizeof(int2),
+                  "flush scratch must fit the (q, A) buffers");
+
+    // Sums the warps' double-float accumulators of one segment in warp order (FP64) and
+    // writes the block's partial row; the accumulators are cleared.  Called by the whole
+    // block at a point where no warp reads the (q, A) buffers that serve as scratch.
     template <int K>
-    __device__ __forceinline__ void flush_warp(float (&hi)[K], float (&lo)[K], double* dst, int lane) {
+    __device__ __forceinline__ void flush_block(float (&hi)[K], float (&lo)[K], double* scratch, double* dst,
+                                                int tid) {
+      const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+      for (int k0 = 0; k0 < K; k0 += kFlushRows) {
+#pragma unroll
+        for (int r = 0; r < kFlushRows; ++r) {
+          if (k0 + r < K) {
+            scratch[(r * kWarps + warp) * 32 + lane] =
+              static_cast<double>(hi[k0 + r]) + static_cast<double>(lo[k0 + r]);
+          }
+        }
+        __syncthreads();
+        const int r = tid >> 5;
+        if (r < kFlushRows && k0 + r < K) {
+          double t = 0.0;
+#pragma unroll
+          for (int w = 0; w < kWarps; ++w) {
+            t += scratch[(r * kWarps + w) * 32 + lane];
+          }
+          dst[(k0 + r) * 32 + lane] = t;
+        }
+        __syncthreads();
+      }
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        dst[k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
-        hi[k]              = 0.0f;
-        lo[k]              = 0.0f;
+        hi[k] = 0.0f;
+        lo[k] = 0.0f;
       }
     }
 
@@ -158,8 +190,10 @@ namespace rg {
         }
         const ItemInfo I = info[st];
         if (I.seg != cur_seg) {
+          // block-uniform (info[st] is shared); every warp is past the previous item's
+          // evaluation (the barrier above), so the (q, A) buffers are free
           if (cur_seg >= 0) {
-            flush_warp<K>(hi, lo, warp_partial(p, b, cur_seg, slice, warp), lane);
+            flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid);
           }
           cur_seg = I.seg;
         }
@@ -217,7 +251,8 @@ namespace rg {
         }
       }
       if (cur_seg >= 0) {
-        flush_warp<K>(hi, lo, warp_partial(p, b, cur_seg, slice, warp), lane);
+        __syncthreads(); // every warp is done reading the last item's (q, A)
+        flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid);
       }
     }
 
@@ -278,7 +313,7 @@ namespace rg {
       }
     }
 
-    // Sums the per-warp partials of every (segment, bin) in (block, warp) order and
+    // Sums the per-block partials of every (segment, bin) in block order and
     // applies the photon-energy factor; masked bins are zero, and every output is
     // NaN if the device status reports a failure.
     struct ReduceParams {
@@ -296,11 +331,12 @@ namespace rg {
       double*         acc64; // when set: acc64 += result in FP64 instead of writing out
     };
 
-    // Block (32 bins x kReduceRows row groups): row group y sums the (block, warp)
-    // partial rows y, y + kReduceRows, ... of its segment, then the row groups are
+    // Block (32 bins x kReduceRows row groups): row group y sums the block partial
+    // rows y, y + kReduceRows, ... of its segment, then the row groups are
     // combined in order through shared memory.  The summation order depends only
     // on the launch geometry, so results are deterministic.
-    constexpr int kReduceRows = 32;
+    constexpr int kReduceRows  = 32;
+    constexpr int kReduceLoads = 8;
 
     __global__ void __launch_bounds__(32 * kReduceRows)
       reduce_partials_kernel(const __grid_constant__ ReduceParams r) {
@@ -320,17 +356,32 @@ namespace rg {
           const int b0    = block_of_item(i0, n_items, r.grid);
           const int b1    = block_of_item(i1 - 1, n_items, r.grid);
           const int slice = bin / kSliceBins, j = bin % kSliceBins;
-          const int rows  = (b1 - b0 + 1) * kWarps;
+          const int rows  = b1 - b0 + 1; // one partial row per block
           const double* base =
-            r.partials + (static_cast<int64_t>(b0 + s) * r.nslices + slice) * kWarps * kSliceBins + j;
-          const int64_t block_stride = static_cast<int64_t>(r.nslices) * kWarps * kSliceBins;
-#pragma unroll 4
-          for (int row = ty; row < rows; row += kReduceRows) {
-            const int bb = row / kWarps, w = row % kWarps;
-            // a block that owns no item (more blocks than items) wrote no partials
-            const int64_t b = b0 + bb;
-            if (b * n_items / r.grid < (b + 1) * n_items / r.grid) {
-              sum += base[bb * block_stride + w * kSliceBins];
+            r.partials + (static_cast<int64_t>(b0 + s) * r.nslices + slice) * kSliceBins + j;
+          const int64_t block_stride = static_cast<int64_t>(r.nslices) * kSliceBins;
+          // a block that owns no item (more blocks than items) wrote no partials; with at
+          // least one item per block every block owns one, and the per-row ownership test
+          // (two 64-bit divisions) is skipped
+          const bool every_block_owns = n_items >= r.grid;
+          // kReduceLoads rows loaded before they are added (in row order, as one at a
+          // time would): the loop is bound by load latency, not by the adds
+          for (int row0 = ty; row0 < rows; row0 += kReduceRows * kReduceLoads) {
+            double v[kReduceLoads];
+#pragma unroll
+            for (int u = 0; u < kReduceLoads; ++u) {
+              const int row = row0 + u * kReduceRows;
+              v[u]          = 0.0;
+              if (row < rows) {
+                const int64_t b = b0 + row;
+                if (every_block_owns || b * n_items / r.grid < (b + 1) * n_items / r.grid) {
+                  v[u] = base[row * block_stride];
+                }
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < kReduceLoads; ++u) {
+              sum += v[u];
             }
           }
         }
@@ -656,7 +707,7 @@ namespace rg {
   } // namespace
 
   int plan_reserve(rg_spectrum_plan* pl, int max_seg) {
-    const size_t need = static_cast<size_t>(pl->grid + max_seg) * pl->nslices * kWarps * kSliceBins;
+    const size_t need = static_cast<size_t>(pl->grid + max_seg) * pl->nslices * kSliceBins;
     if (need > pl->partial_cap) {
       cudaFree(pl->d_partials);
       pl->d_partials = nullptr;
@@ -883,21 +934,7 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_partials);
   cudaFree(pl->d_prefix);
   cudaFree(pl->d_plain_acc);
-  for (float* b : pl->d_stage) {
-    cudaFree(b);
-  }
   cudaFree(pl->d_acc64);
-  for (int b = 0; b < rg_spectrum_plan::kStageBuffers; ++b) {
-    if (pl->copied[b]) {
-      cudaEventDestroy(pl->copied[b]);
-    }
-    if (pl->consumed[b]) {
-      cudaEventDestroy(pl->consumed[b]);
-    }
-  }
-  if (pl->copy_stream) {
-    cudaStreamDestroy(pl->copy_stream);
-  }
   for (auto* v : { &pl->ev_used, &pl->ev_free }) {
     for (auto& e : *v) {
       cudaEventDestroy(e.first);
@@ -1003,46 +1040,42 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
   if (pl->nbins == 0) {
     return RG_OK;
   }
-  auto              s           = static_cast<cudaStream_t>(stream);
+  auto s = static_cast<cudaStream_t>(stream);
+  if (!pl->d_acc64) {
+    RG_CUDA_TRY(cudaMalloc(&pl->d_acc64, sizeof(double) * pl->nbins));
+  }
   // 2^22-particle chunks, double-buffered (each chunk costs a kernel tail and a reduction,
   // so chunks are kept large; 2^21-particle chunks and a third buffer were measured slower
   // or no faster)
-  constexpr int64_t kStageChunk = int64_t(1) << 22;
-  constexpr int     kBuffers    = rg_spectrum_plan::kStageBuffers;
-  if (!pl->d_stage[0]) {
-    for (int b = 0; b < kBuffers; ++b) {
-      RG_CUDA_TRY(cudaMalloc(&pl->d_stage[b], sizeof(float) * rg::kComps * kStageChunk));
-      RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->copied[b], cudaEventDisableTiming));
-      RG_CUDA_TRY(cudaEventCreateWithFlags(&pl->consumed[b], cudaEventDisableTiming));
-    }
-    RG_CUDA_TRY(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
-    RG_CUDA_TRY(cudaMalloc(&pl->d_acc64, sizeof(double) * pl->nbins));
-    pl->stage_chunk = kStageChunk;
-  }
-  const float* host[rg::kComps];
+  rg::HostStaging* st = nullptr;
+  RG_TRY(rg::host_staging(&st));
+  constexpr int64_t kStageChunk = rg::HostStaging::kChunk;
+  constexpr int     kBuffers    = rg::HostStaging::kBuffers;
+  const float*      host[rg::kComps];
   rg::particle_comps(p, host);
   RG_CUDA_TRY(cudaMemsetAsync(pl->d_acc64, 0, sizeof(double) * pl->nbins, s));
-  // consumed[b] was last recorded after the kernel that read staging buffer b (by an
-  // earlier call of this plan, or never): the first copies of this call wait for
-  // exactly that, so they overlap the tail of the previous call's kernels
-  const int64_t n = p->n;
-  for (int64_t c = 0, a = 0; a < n; ++c, a += kStageChunk) {
-    const int     b = static_cast<int>(c % kBuffers);
+  // consumed[b] was last recorded after the kernel that read staging buffer b (in an
+  // earlier call on this device, by any plan, or never): the first copies of this call
+  // wait for exactly that, so they overlap the tail of the previous call's kernels
+  std::lock_guard<std::mutex> lock(st->mu);
+  const int64_t               n = p->n;
+  for (int64_t a = 0; a < n; a += kStageChunk) {
+    const int     b = static_cast<int>(st->issued++ % kBuffers);
     const int64_t m = std::min(kStageChunk, n - a);
-    RG_CUDA_TRY(cudaStreamWaitEvent(pl->copy_stream, pl->consumed[b], 0));
+    RG_CUDA_TRY(cudaStreamWaitEvent(st->copy_stream, st->consumed[b], 0));
     const float* dev[rg::kComps] = {};
     for (int k = 0; k < rg::kComps; ++k) {
       if (host[k]) {
-        float* dst = pl->d_stage[b] + k * kStageChunk;
+        float* dst = st->d_stage[b] + k * kStageChunk;
         RG_CUDA_TRY(cudaMemcpyAsync(dst, host[k] + a, sizeof(float) * m, cudaMemcpyHostToDevice,
-                                    pl->copy_stream));
+                                    st->copy_stream));
         dev[k] = dst;
       }
     }
-    RG_CUDA_TRY(cudaEventRecord(pl->copied[b], pl->copy_stream));
-    RG_CUDA_TRY(cudaStreamWaitEvent(s, pl->copied[b], 0));
+    RG_CUDA_TRY(cudaEventRecord(st->copied[b], st->copy_stream));
+    RG_CUDA_TRY(cudaStreamWaitEvent(s, st->copied[b], 0));
     RG_TRY(rg::run_fused(pl, dev, nullptr, m, 1, out, s, pl->d_acc64));
-    RG_CUDA_TRY(cudaEventRecord(pl->consumed[b], s));
+    RG_CUDA_TRY(cudaEventRecord(st->consumed[b], s));
   }
   rg::finalize_acc_kernel<<<(pl->nbins + 255) / 256, 256, 0, s>>>(pl->d_acc64, pl->nbins, pl->d_status,
                                                                   out);

@@ -18,7 +18,6 @@ namespace rg {
   constexpr int kSliceBins   = 512; // bins per block slice (K <= 16 rows of 32)
   constexpr int kChunk       = 512; // particles per work item
   constexpr int kChunkPad    = kChunk + 4;
-  constexpr int kComps       = 10;  // u0 u1 u2 e0 e1 e2 b0 b1 b2 w
   constexpr int kBlocksPerSM = 2;
 
   // extra status bit: segment offsets were not non-decreasing / within [0, n]
@@ -53,7 +52,7 @@ namespace rg {
     const float4*  htable;
     int            hseg;
     int            frac;
-    double*        partials;     // [(grid + nseg) * nslices * kWarps * kSliceBins]
+    double*        partials;     // [(grid + nseg) * nslices * kSliceBins]
     int            nslices;
     unsigned*      status;
     // Always 0 (zero-initialised with the struct).  The kernel builds an integer
@@ -296,10 +295,9 @@ namespace rg {
     return __uint_as_float(fb) * 0x1p126f;
   }
 
-  __device__ __forceinline__ double* warp_partial(const FusedParams& p, int b, int seg, int slice,
-                                                  int warp) {
-    return p.partials +
-           ((static_cast<int64_t>(b + seg) * p.nslices + slice) * kWarps + warp) * kSliceBins;
+  // The FP64 partial row of block b for segment seg (kSliceBins per slice).
+  __device__ __forceinline__ double* block_partial(const FusedParams& p, int b, int seg, int slice) {
+    return p.partials + (static_cast<int64_t>(b + seg) * p.nslices + slice) * kSliceBins;
   }
 
 } // namespace rg

@@ -1,6 +1,5 @@
 // rg_spectrum_plan: the host-side state of a prepared spectrum (photon bins in
-// fixed-point table coordinates, scalars, scratch, streams for host-resident
-// runs).  Shared by spectrum.cu and adjoint.cu.
+// fixed-point table coordinates, scalars, scratch).  Shared by spectrum.cu and adjoint.cu.
 #pragma once
 
 #include "rg_internal.hpp"
@@ -43,14 +42,8 @@ struct rg_spectrum_plan {
   // kernel timing (events bracketing each fused launch)
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
-  // host-resident streaming: device staging for two chunks, a copy stream
-  // host-streaming staging: kStageBuffers device buffers of stage_chunk particles (all components)
-  static constexpr int kStageBuffers = 2;
-  float*       d_stage[kStageBuffers]  = {};
-  int64_t      stage_chunk = 0;
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t  copied[kStageBuffers]   = {};
-  cudaEvent_t  consumed[kStageBuffers] = {};
+  // host-resident runs: FP64 spectrum accumulated over the staged chunks (the staging
+  // buffers and copy stream belong to the device, rg::HostStaging)
   double*      d_acc64     = nullptr;
 };
 
