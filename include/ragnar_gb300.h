@@ -314,7 +314,9 @@ int rg_energy_thresholds(const float* bins, int32_t nbins, int32_t fourvel, floa
  * or sqrt(1+u^2); bin index always from log10 (even for linear bins), clamped
  * into [0, n-1]; hist[k] = sum 1/energy (log_spaced) or the count.  bins is host
  * (nbins); hist is nbins device floats; counts (nullable) receives exact
- * uint64 counts per bin. */
+ * uint64 counts per bin.  Stream-ordered: returns once the work is enqueued (the
+ * bin thresholds are cached on the device per bin set, so no host buffer is read
+ * after the call returns). */
 int rg_energy_distribution(const float* ux, const float* uy, const float* uz, int64_t n,
                            const float* bins, int32_t nbins, int32_t log_spaced,
                            int32_t fourvel, float* hist, uint64_t* counts, void* stream);

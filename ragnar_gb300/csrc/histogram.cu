@@ -258,48 +258,112 @@ namespace rg {
       ref_energy_index(std::numeric_limits<float>::quiet_NaN(), fourvel, emin, emax, n));
   }
 
-  // Thresholds of recently used bin sets (the host binary search costs far more
-  // than the histogram kernel for small particle counts); keyed on the bin values
-  // and the energy definition, at most kThrCacheEntries kept.
-  struct ThrEntry {
-    std::vector<float> bins, thr;
-    bool               fourvel = true;
-    int                nan_index = 0;
-    float              emin = 0, emax = 0;
-  };
+  namespace {
 
-  void cached_thresholds(const float* bins, int n, bool fourvel, std::vector<float>& thr, int& nan_index,
-                         float& emin, float& emax) {
-    constexpr std::size_t         kThrCacheEntries = 16;
-    static std::mutex             mu;
-    static std::vector<ThrEntry>  cache; // most recent last
-    {
-      std::lock_guard<std::mutex> lock(mu);
-      for (auto it = cache.begin(); it != cache.end(); ++it) {
-        if (it->fourvel == fourvel && static_cast<int>(it->bins.size()) == n &&
-            std::memcmp(it->bins.data(), bins, sizeof(float) * n) == 0) {
-          thr       = it->thr;
-          nan_index = it->nan_index;
-          emin      = it->emin;
-          emax      = it->emax;
-          std::rotate(it, it + 1, cache.end());
-          return;
-        }
+    // Thresholds of recently used bin sets (the host binary search costs far more
+    // than the histogram kernel for small particle counts), with one device copy per
+    // GPU that used them, so a call copies nothing to the device and need not wait
+    // for a host buffer; keyed on the bin values and the energy definition, at most
+    // kThrCacheEntries kept.
+    struct ThrEntry {
+      std::vector<float>                  bins, thr;
+      bool                                fourvel   = true;
+      int                                 nan_index = 0;
+      float                               emin = 0, emax = 0;
+      std::vector<std::pair<int, float*>> dev; // (device, thresholds on that device)
+    };
+
+    constexpr std::size_t kThrCacheEntries = 16;
+
+    std::mutex& thr_mutex() {
+      static std::mutex m;
+      return m;
+    }
+
+    std::vector<ThrEntry>& thr_cache() { // most recent last
+      static std::vector<ThrEntry> c;
+      return c;
+    }
+
+    // Frees the device copies of an entry; a kernel of any stream may still read them,
+    // so each device is synchronised first (entries are evicted rarely).
+    void free_entry(ThrEntry& e) {
+      int cur = 0;
+      cudaGetDevice(&cur);
+      for (auto& d : e.dev) {
+        cudaSetDevice(d.first);
+        cudaDeviceSynchronize();
+        cudaFree(d.second);
+      }
+      cudaSetDevice(cur);
+      e.dev.clear();
+    }
+
+  } // namespace
+
+  // Thresholds of a bin set on the current device (host values in `thr` when wanted).
+  int device_thresholds(const float* bins, int n, bool fourvel, const float** d_thr, int& nan_index,
+                        float& emin, float& emax, std::vector<float>* thr) {
+    int device = 0;
+    RG_CUDA_TRY(cudaGetDevice(&device));
+    std::lock_guard<std::mutex> lock(thr_mutex());
+    auto&                       cache = thr_cache();
+    auto                        it    = cache.begin();
+    for (; it != cache.end(); ++it) {
+      if (it->fourvel == fourvel && static_cast<int>(it->bins.size()) == n &&
+          std::memcmp(it->bins.data(), bins, sizeof(float) * n) == 0) {
+        break;
       }
     }
-    energy_thresholds(bins, n, fourvel, thr, nan_index, emin, emax);
-    ThrEntry e;
-    e.bins.assign(bins, bins + n);
-    e.thr       = thr;
-    e.fourvel   = fourvel;
-    e.nan_index = nan_index;
-    e.emin      = emin;
-    e.emax      = emax;
-    std::lock_guard<std::mutex> lock(mu);
-    if (cache.size() >= kThrCacheEntries) {
-      cache.erase(cache.begin());
+    if (it == cache.end()) {
+      ThrEntry e;
+      energy_thresholds(bins, n, fourvel, e.thr, e.nan_index, e.emin, e.emax);
+      e.bins.assign(bins, bins + n);
+      e.fourvel = fourvel;
+      if (cache.size() >= kThrCacheEntries) {
+        free_entry(cache.front());
+        cache.erase(cache.begin());
+      }
+      cache.push_back(std::move(e));
+      it = cache.end() - 1;
+    } else {
+      std::rotate(it, it + 1, cache.end());
+      it = cache.end() - 1;
     }
-    cache.push_back(std::move(e));
+    ThrEntry& e = *it;
+    float*    p = nullptr;
+    for (auto& d : e.dev) {
+      if (d.first == device) {
+        p = d.second;
+      }
+    }
+    if (!p && d_thr) {
+      RG_CUDA_TRY(cudaMalloc(&p, sizeof(float) * n));
+      const cudaError_t err = cudaMemcpy(p, e.thr.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) {
+        cudaFree(p);
+        return cuda_error(err, "threshold copy");
+      }
+      e.dev.emplace_back(device, p);
+    }
+    if (d_thr) {
+      *d_thr = p;
+    }
+    if (thr) {
+      *thr = e.thr;
+    }
+    nan_index = e.nan_index;
+    emin      = e.emin;
+    emax      = e.emax;
+    return RG_OK;
+  }
+
+  void free_threshold_cache() {
+    std::lock_guard<std::mutex> lock(thr_mutex());
+    for (auto& e : thr_cache()) {
+      free_entry(e);
+    }
+    thr_cache().clear();
   }
 
 } // namespace rg
@@ -332,11 +396,11 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
   if (nbins > rg::kHistMaxBins) {
     return rg::set_error(RG_ERR_UNSUPPORTED, "energyDistribution supports at most 4096 bins");
   }
-  auto               s = static_cast<cudaStream_t>(stream);
-  std::vector<float> thr;
-  int                nan_index = 0;
-  float              emin, emax;
-  rg::cached_thresholds(bins, nbins, fourvel != 0, thr, nan_index, emin, emax);
+  auto         s         = static_cast<cudaStream_t>(stream);
+  const float* d_thr     = nullptr;
+  int          nan_index = 0;
+  float        emin, emax;
+  RG_TRY(rg::device_thresholds(bins, nbins, fourvel != 0, &d_thr, nan_index, emin, emax, nullptr));
 
   rg::DeviceContext* ctx = nullptr;
   RG_TRY(rg::context(&ctx));
@@ -352,13 +416,11 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
   const int64_t want = std::max<int64_t>(1, (n + 4095) / 4096);
   const int     G    = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(ctx->sms) * per_sm));
 
-  // one allocation for thresholds and per-block partials, freed stream-ordered
-  const size_t off_pc = 256 * ((sizeof(float) * nbins + 255) / 256);
-  const size_t off_ps = off_pc + sizeof(unsigned long long) * static_cast<size_t>(G) * nbins;
-  const size_t bytes  = off_ps + sizeof(double) * static_cast<size_t>(G) * nbins;
-  unsigned char* buf  = nullptr;
+  // one stream-ordered allocation for the per-block partials
+  const size_t   off_ps = sizeof(unsigned long long) * static_cast<size_t>(G) * nbins;
+  const size_t   bytes  = off_ps + sizeof(double) * static_cast<size_t>(G) * nbins;
+  unsigned char* buf    = nullptr;
   RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
-  RG_CUDA_TRY(cudaMemcpyAsync(buf, thr.data(), sizeof(float) * nbins, cudaMemcpyHostToDevice, s));
 
   rg::HistParams p {};
   p.ux         = ux;
@@ -368,7 +430,7 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
   p.nbins      = nbins;
   p.fourvel    = fourvel ? 1 : 0;
   p.log_spaced = log_spaced ? 1 : 0;
-  p.thr        = reinterpret_cast<const float*>(buf);
+  p.thr        = d_thr;
   p.nan_index  = nan_index;
   // estimate: index ~ (n-1) log(E/emin) / log(emax/emin), log2(E) = log2(E^2) / 2
   const double span = std::log2(static_cast<double>(emax) / static_cast<double>(emin));
@@ -379,7 +441,7 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
     p.est_a = 0.0f;
     p.est_c = 0.0f;
   }
-  p.part_counts = reinterpret_cast<unsigned long long*>(buf + off_pc);
+  p.part_counts = reinterpret_cast<unsigned long long*>(buf);
   p.part_sums   = reinterpret_cast<double*>(buf + off_ps);
   rg::histogram_kernel<<<G, rg::kHistThreads, smem, s>>>(p);
   RG_CUDA_TRY(cudaGetLastError());
@@ -388,8 +450,6 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
     reinterpret_cast<unsigned long long*>(counts));
   RG_CUDA_TRY(cudaGetLastError());
   RG_CUDA_TRY(cudaFreeAsync(buf, s));
-  // thr (host) must outlive the asynchronous copy above
-  RG_CUDA_TRY(cudaStreamSynchronize(s));
   return RG_OK;
 }
 

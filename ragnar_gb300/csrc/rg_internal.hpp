@@ -105,6 +105,8 @@ namespace rg {
   int build_smooth_table(SmoothTable& t, cudaStream_t s);
   void free_tables(DeviceContext& c);
   void free_staging(DeviceContext& c);
+  // Device copies of the histogram's bin thresholds (histogram.cu).
+  void free_threshold_cache();
 
   // Host grids with the reference's float/double arithmetic.
   float logspace_point(float start, float stop, std::size_t num, std::size_t i);

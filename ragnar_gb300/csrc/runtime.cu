@@ -165,6 +165,7 @@ int rg_init(int device) {
 }
 
 int rg_finalize(void) {
+  rg::free_threshold_cache();
   std::lock_guard<std::mutex> lock(rg::ctx_mutex());
   for (auto& kv : rg::contexts()) {
     int cur = 0;

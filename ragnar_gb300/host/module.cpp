@@ -323,6 +323,8 @@ namespace rgh {
         check(rg_energy_distribution(v2.u[0], v2.u[1], v2.u[2], v.n, hb.data(),
                                      static_cast<int32_t>(hb.size()), bins.log_spaced ? 1 : 0,
                                      fourvel ? 1 : 0, hist.data(), nullptr, nullptr));
+        // the reference fences before returning (particles.cpp:256)
+        check(rg_stream_synchronize(nullptr));
       }
     }
     if (g_verbose) {
