@@ -14,8 +14,8 @@
 // correctly rounded reciprocal of sqrtf(Usqr) (double rounding of one division
 // of floats through double is innocuous); for sqrt(1 + Usqr) energies it is a
 // double-float Newton step of rsqrt rounded to float.  Sums are accumulated in
-// FP32 shared-memory bins flushed to FP64 every chunk, then across blocks in
-// FP64 in a fixed order.
+// FP32 shared-memory bins (kSumCopies lane-indexed copies) flushed to FP64 every
+// chunk, then across blocks in FP64 in a fixed order.
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
 
@@ -31,6 +31,11 @@ namespace rg {
   namespace {
 
     constexpr int kHistThreads   = 256;
+    // Copies of the FP32 sum bins, lane l adding into copy l mod kSumCopies: the float
+    // shared-memory add retries while lanes of a warp hit the same bin, and energies
+    // of a power law crowd a few bins (4 copies: 0.155 ms against 0.179 ms per call on
+    // 3.3e7 particles; 16 copies were slower).
+    constexpr int kSumCopies     = 4;
     constexpr int kHistMaxBins   = 4096;
     constexpr int kFlushParticles = 4096; // per block between FP32 -> FP64 flushes
 
@@ -110,15 +115,19 @@ namespace rg {
       const int nb      = p.nbins;
       float*    thr     = reinterpret_cast<float*>(smem);
       unsigned* cnt     = reinterpret_cast<unsigned*>(thr + nb);
-      float*    sum32   = reinterpret_cast<float*>(cnt + nb);
-      double*   sum64   = reinterpret_cast<double*>(smem + ((3 * sizeof(float) * nb + 15) & ~size_t(15)));
+      constexpr int kC = kSumCopies;
+      float*    sum32   = reinterpret_cast<float*>(cnt + nb); // [kC][nb]
+      double*   sum64   = reinterpret_cast<double*>(smem + (((2 + kC) * sizeof(float) * nb + 15) & ~size_t(15)));
       for (int i = threadIdx.x; i < nb; i += blockDim.x) {
         thr[i]   = p.thr[i];
         cnt[i]   = 0u;
-        sum32[i] = 0.0f;
         sum64[i] = 0.0;
       }
+      for (int i = threadIdx.x; i < kC * nb; i += blockDim.x) {
+        sum32[i] = 0.0f;
+      }
       __syncthreads();
+      float* sum_l = sum32 + (threadIdx.x & (kC - 1)) * nb;
 
       // contiguous range of particles per block, in rounds of kFlushParticles
       const int64_t G       = gridDim.x;
@@ -146,7 +155,7 @@ namespace rg {
             } else {
               v = __frcp_rn(sqrtf(U)); // 0 -> inf, inf -> 0, NaN -> NaN
             }
-            atomicAdd(&sum32[k], v);
+            atomicAdd(&sum_l[k], v);
           }
         };
         if (vec_ok) {
@@ -173,8 +182,12 @@ namespace rg {
         if (p.log_spaced) {
           __syncthreads();
           for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-            sum64[i] += static_cast<double>(sum32[i]);
-            sum32[i] = 0.0f;
+            double t = sum64[i];
+            for (int c = 0; c < kC; ++c) {
+              t += static_cast<double>(sum32[c * nb + i]);
+              sum32[c * nb + i] = 0.0f;
+            }
+            sum64[i] = t;
           }
         }
         __syncthreads();
@@ -404,7 +417,8 @@ int rg_energy_distribution(const float* ux, const float* uy, const float* uz, in
 
   rg::DeviceContext* ctx = nullptr;
   RG_TRY(rg::context(&ctx));
-  const size_t smem = ((3 * sizeof(float) * nbins + 15) & ~size_t(15)) + sizeof(double) * nbins;
+  const size_t smem =
+    (((2 + rg::kSumCopies) * sizeof(float) * nbins + 15) & ~size_t(15)) + sizeof(double) * nbins;
   if (smem > 48 * 1024) {
     RG_CUDA_TRY(cudaFuncSetAttribute(rg::histogram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));
