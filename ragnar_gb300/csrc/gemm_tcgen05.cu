@@ -23,8 +23,9 @@
 // left operand (the distributions, FP32) is read by eight converter warps, split
 // exactly into its BF16 terms and written straight into 128-byte-swizzled shared
 // tiles, double-buffered per 64-gamma block: no split kernel and no BF16 copy in
-// HBM.  The k loop runs gamma block outer, product inner, so each converted tile
-// serves every product that uses it.  One thread issues tcgen05.mma (M 128, N =
+// HBM.  The k loop runs gamma block outer, right term inner, and every product of
+// a resident right term runs before its ring stage is released, so each converted
+// left tile and each streamed right tile serves every product that uses it.  One thread issues tcgen05.mma (M 128, N =
 // tile width, K 16) and commits each ring stage back to the producer and each
 // left buffer back to the converters; after the last commit warps 0..3 read both
 // accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
@@ -61,9 +62,10 @@ namespace rg {
     constexpr GemmConfig kConfigs[] = { { 256, 4 }, { 128, 6 }, { 128, 4 } };
     constexpr int        kNumConfigs = 3;
     constexpr unsigned kDevGemmTimeout = 8u;
-    // products h.h, h.m, m.h, h.l, l.h, m.m: stored term (0 h, 1 m, 2 l) of each operand
-    __constant__ int kLeft[6]  = { 0, 0, 1, 0, 2, 1 };
-    __constant__ int kRight[6] = { 0, 1, 0, 2, 0, 1 };
+    // Products of stored terms (0 h, 1 m, 2 l): every (left L, right R) with L + R < nstore,
+    // i.e. h.h, m.h, l.h, h.m, m.m, h.l for 3 stored terms and h.h, m.h, h.m for 2.  The
+    // ring streams each right term of a gamma block once, and every product that uses it
+    // runs while it is resident.
 
     __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y,
                                                 uint64_t* bar) {
@@ -196,7 +198,7 @@ namespace rg {
 
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
-      const int nk = g.nprod * g.kpt; // k loop: gamma block outer, product inner
+      const int nk = g.nstore * g.kpt; // ring: gamma block outer, right term inner
 
       if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -232,10 +234,10 @@ namespace rg {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
-          // product t multiplies left term kLeft[t] by right term kRight[t] of gamma block gb
-          const int gb = kb / g.nprod, t = kb - gb * g.nprod;
+          // right term r of gamma block gb
+          const int gb = kb / g.nstore, r = kb - gb * g.nstore;
           mbar_arrive_expect_tx(&b_full[s], kBytesB);
-          tma_load_2d(sB + s * kBytesB, &tmB, (kRight[t] * g.kpt + gb) * kBK, n0, &b_full[s]);
+          tma_load_2d(sB + s * kBytesB, &tmB, (r * g.kpt + gb) * kBK, n0, &b_full[s]);
         }
       } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer -------------------------------------------------------------------
@@ -247,8 +249,8 @@ namespace rg {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
-          for (int t = 0; t < g.nprod; ++t) {
-            const int      kb = gb * g.nprod + t;
+          for (int r = 0; r < g.nstore; ++r) {
+            const int      kb = gb * g.nstore + r;
             const int      s  = kb % kStages;
             const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
             if (!mbar_wait_bounded(&b_full[s], ph)) {
@@ -257,17 +259,19 @@ namespace rg {
               break;
             }
             tc_fence_after();
-            const uint64_t da  = smem_desc_sw128(sA + (ab * g.nstore + kLeft[t]) * kBytesTerm);
-            const uint64_t db  = smem_desc_sw128(sB + s * kBytesB);
-            const uint32_t acc = t == 0 ? 0u : 1u;
+            const uint64_t db = smem_desc_sw128(sB + s * kBytesB);
+            for (int L = 0; L + r < g.nstore; ++L) {
+              const uint64_t da  = smem_desc_sw128(sA + (ab * g.nstore + L) * kBytesTerm);
+              const uint32_t acc = (L == 0 && r == 0) ? 0u : 1u; // h.h alone in accumulator 0
 #pragma unroll
-            for (int k = 0; k < kBK / kUmmaK; ++k) {
-              // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
-              mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k), kIdesc,
-                       ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
+              for (int k = 0; k < kBK / kUmmaK; ++k) {
+                // advance along K inside the 128-byte swizzle row: 32 bytes = 2 in the >> 4 field
+                mma_bf16(tmem_d + acc * kBN, da + uint64_t(2 * k), db + uint64_t(2 * k), kIdesc,
+                         ((started >> acc) & 1u) | (k > 0 ? 1u : 0u));
+              }
+              started |= 1u << acc;
             }
-            started |= 1u << acc;
-            mma_commit(&b_empty[s]);
+            mma_commit(&b_empty[s]); // the stage is free once every product using it completes
           }
           mma_commit(&a_empty[ab]); // the left tiles of gamma block gb are free once these MMAs complete
         }
