@@ -11,9 +11,13 @@
 //     matters (e in [g/2, g]), so t avoids the reference's 1 - e/g cancellation;
 //   q = t / Gamma = (t / g) (1 / (4 e_s));  e <= g Gamma / (1 + Gamma)  <=>  q <= 1 (e < g);
 //   KN = q (2 ln 2) log2 q + ((1 + h) + (1 - h) q - 2 q^2),  h = t^2 / (2 (1 + t)).
-// Per eval: FMUL (q), MUFU.LG2, FMUL + FFMA (log term), two FFMA (quadratic), select of KN
-// (q <= 1), FFMA into the FP32 accumulator.  q >= 1e-30 is guaranteed by a floor on t/g set
-// per (e, g) from the smallest 1 / (4 e_s), so the log's argument is always a normal float.
+// With L = 2 ln 2 and p = L q (so 2 q ln q = p log2 q = p (log2 p - log2 L)) this is
+//   KN = p log2 p + ((1 + h) + ((1 - h) / L - log2 L) p - (2 / L^2) p^2),
+// whose quadratic's coefficients depend on (e, g) only and are set once per item.
+// Per eval: FMUL (p = (L t / g) (1 / (4 e_s))), MUFU.LG2, two FFMA (quadratic), FFMA (log
+// term), select of KN (q <= 1, i.e. p <= L), FFMA into the FP32 accumulator.  q >= 1e-30 is
+// guaranteed by a floor on t/g set per (e, g) from the smallest 1 / (4 e_s), so the log's
+// argument is always a normal float.
 //
 // Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
 // (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
@@ -89,7 +93,10 @@ namespace rg {
         hi[k] = 0.0f;
         lo[k] = 0.0f;
       }
-      const float two_ln2 = 1.3862943611198906f;
+      // L = 2 ln 2 rounded to FP32; log2 L and -2 / L^2 of that FP32 value
+      const float kL     = 1.3862943649291992f;
+      const float kLog2L = 0.47123363101939075f;
+      const float kC2    = -1.0406844847835448f;
       // t/g >= this keeps q = (t/g) / (4 e_s) >= 1e-30 for every soft photon with e_s > 0:
       // the log's argument stays a normal float without a per-eval clamp
       const float tg_floor = __fdiv_rn(1e-30f, *p.inv4es_min);
@@ -105,7 +112,7 @@ namespace rg {
         }
         const float inv_g = __frcp_rn(gv);
         // per (e, g): t / g, 1 + h, 1 - h; q = (t / g) / (4 e_s) > 1 marks no contribution
-        float tg[K], A0[K], A1[K], acc[K];
+        float pg[K], A0[K], B1[K], acc[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
           const float e = energy(k);
@@ -117,9 +124,9 @@ namespace rg {
           } else {
             t = 3.0e38f; // q = huge: every soft photon fails q <= 1
           }
-          tg[k]  = fmaxf(__fmul_rn(t, inv_g), tg_floor);
+          pg[k]  = __fmul_rn(kL, fmaxf(__fmul_rn(t, inv_g), tg_floor)); // p = pg / (4 e_s)
           A0[k]  = __fadd_rn(1.0f, h);
-          A1[k]  = __fsub_rn(1.0f, h);
+          B1[k]  = __fsub_rn(__fdiv_rn(__fsub_rn(1.0f, h), kL), kLog2L);
           acc[k] = 0.0f;
         }
         for (int s = s0; s < s1; ++s) {
@@ -127,13 +134,13 @@ namespace rg {
           const float w  = __ldg(p.ws + s);
 #pragma unroll
           for (int k = 0; k < K; ++k) {
-            const float q  = __fmul_rn(tg[k], i4);
-            // q >= 1e-30 by the floor on t/g (q ln q < 1e-28 below it), so the log's argument
-            // is a normal float; q > 1 (or NaN) selects 0 whatever KN evaluated to
-            const float lq   = lg2_normal(q);
-            const float poly = __fmaf_rn(__fmaf_rn(-2.0f, q, A1[k]), q, A0[k]);
-            const float kn   = __fmaf_rn(__fmul_rn(q, two_ln2), lq, poly);
-            acc[k]           = __fmaf_rn(w, q <= 1.0f ? kn : 0.0f, acc[k]);
+            const float pq = __fmul_rn(pg[k], i4);
+            // p >= L 1e-30 by the floor on t/g, so the log's argument is a normal float;
+            // p > L (q > 1) or NaN selects 0 whatever KN evaluated to
+            const float lp   = lg2_normal(pq);
+            const float poly = __fmaf_rn(__fmaf_rn(kC2, pq, B1[k]), pq, A0[k]);
+            const float kn   = __fmaf_rn(pq, lp, poly);
+            acc[k]           = __fmaf_rn(w, pq <= kL ? kn : 0.0f, acc[k]);
           }
         }
         // scale by e^2 f_g / g^k and fold into the double-float sums
