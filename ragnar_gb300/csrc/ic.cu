@@ -22,7 +22,8 @@
 // Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
 // (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
 // e^2 f_g / g^k and folded into a double-float; per-warp FP64 partials are reduced in a
-// fixed order by a second kernel (deterministic).  Non-positive or non-finite IC bins give
+// fixed order: the block's warps in FP64 at its end, then the blocks by a second kernel
+// (deterministic).  Non-positive or non-finite IC bins give
 // 0 (the reference produces NaN there).
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
@@ -51,7 +52,7 @@ namespace rg {
       const float* eic;     // ne IC photon energies
       int          ne;
       int          nslices;
-      double*      partials; // [grid][nslices][kIcWarps][kIcSlice]
+      double*      partials; // [grid][nslices][kIcSlice]: one row per block
     };
 
     // inv4es, ws and the smallest positive inv4es (positive floats order like their bit
@@ -154,14 +155,25 @@ namespace rg {
           lo[k]            = __fadd_rn(lo[k], sm.lo);
         }
       }
-      double* dst = p.partials + ((b * p.nslices + slice) * kIcWarps + warp) * kIcSlice;
+      // the block's warps summed in FP64 in warp order: one partial row per block
+      __shared__ double red[kIcWarps * kIcSlice];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        dst[k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
+        red[warp * kIcSlice + k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
+      }
+      __syncthreads();
+      double* dst = p.partials + (b * p.nslices + slice) * kIcSlice;
+      for (int j = threadIdx.x; j < K * 32; j += kIcThreads) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kIcWarps; ++w) {
+          t += red[w * kIcSlice + j];
+        }
+        dst[j] = t;
       }
     }
 
-    // out[e] = sum over blocks and warps (fixed order) of the partials; 32 bins x 32 row groups.
+    // out[e] = sum over blocks (fixed order) of the partial rows; 32 bins x 32 row groups.
     __global__ void __launch_bounds__(1024)
       ic_reduce_kernel(const double* __restrict__ partials, int grid, int nslices, int ne, float* __restrict__ out) {
       __shared__ double part[32][33];
@@ -169,12 +181,10 @@ namespace rg {
       double    sum = 0.0;
       if (bin < ne) {
         const int slice = bin / kIcSlice, j = bin % kIcSlice;
-        const int rows  = grid * kIcWarps;
         // unrolled so that several rows' loads are in flight (the adds stay in row order)
 #pragma unroll 8
-        for (int r = ty; r < rows; r += 32) {
-          const int blk = r / kIcWarps, w = r % kIcWarps;
-          sum += partials[((static_cast<int64_t>(blk) * nslices + slice) * kIcWarps + w) * kIcSlice + j];
+        for (int r = ty; r < grid; r += 32) {
+          sum += partials[(static_cast<int64_t>(r) * nslices + slice) * kIcSlice + j];
         }
       }
       part[ty][threadIdx.x] = sum;
@@ -239,7 +249,7 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   const size_t off_ws   = 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_min  = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_part = off_min + 256;
-  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * rg::kIcWarps * rg::kIcSlice;
+  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * rg::kIcSlice;
   unsigned char* buf    = nullptr;
   RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
   rg::IcParams p {};
