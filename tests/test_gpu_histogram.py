@@ -124,3 +124,15 @@ def test_full_size_counts_conserved(gpu):
     np.testing.assert_array_equal(c, c1 + c2)
     m = h > 0
     assert np.max(np.abs(h1[m] + h2[m] - h[m]) / h[m]) < 1e-6
+
+
+def test_threshold_cache_eviction(gpu, oracle_lib):
+    """More bin sets than the device threshold cache keeps (16): evicted sets are rebuilt
+    and every call still matches the oracle bit for bit."""
+    P = particles(20000, seed=33)
+    for rep in range(2):
+        for i in range(20):
+            bins = oracle_lib.logspace(1e-2 * (1.0 + 0.01 * i), 1e3, 50 + i)
+            h, c = gpu_hist(P["ux"], P["uy"], P["uz"], bins, True, True, gpu)
+            _, h64, cnt = oracle_lib.energy_distribution(P["ux"], P["uy"], P["uz"], bins, True, True)
+            np.testing.assert_array_equal(c, cnt)
