@@ -312,3 +312,22 @@ def test_host_streaming_chunks_across_plans(gpu, oracle_lib):
         plans[i % 2].check()
         # same items and warps; only the FP64 order of the block partials differs
         assert max_rel(first[i].double().cpu().numpy(), res.double().cpu().numpy()) <= 1e-6
+
+
+def test_host_streaming_pageable_memory(gpu, oracle_lib, table):
+    """Pageable (not pinned) host arrays go through the same call; the result equals the
+    pinned-input result bit for bit."""
+    P = particles(5000, seed=77, bfield="iso", weights=True)
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    A = {k: np.ascontiguousarray(v) for k, v in P.items()}
+    prt = capi.host_particles([A["ux"], A["uy"], A["uz"]], b=[A["bx"], A["by"], A["bz"]], w=A["w"], n=5000)
+    out = torch.empty(200, device=gpu)
+    plan.run_host(prt, out)
+    plan.check()
+    H, hprt = host_particles(P)
+    out2 = torch.empty(200, device=gpu)
+    plan.run_host(hprt, out2)
+    plan.check()
+    assert torch.equal(out, out2)
+    assert max_rel(out.cpu().numpy(), oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)) <= SPECTRUM_RTOL
