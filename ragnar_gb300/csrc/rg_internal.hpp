@@ -82,6 +82,10 @@ namespace rg {
     cudaEvent_t  consumed[kBuffers] = {};
     cudaStream_t copy_stream        = nullptr;
     uint64_t     issued             = 0; // chunks issued so far; chunk c uses buffer c % kBuffers
+    HostStaging() = default;
+    HostStaging(const HostStaging&) = delete;
+    HostStaging& operator=(const HostStaging&) = delete;
+    ~HostStaging(); // waits for its copies and kernels, then releases everything it holds
   };
 
   struct DeviceContext {

@@ -16,9 +16,11 @@ namespace rg {
       return m;
     }
 
+    // Never destroyed: releasing device resources from a static destructor at process exit
+    // would call the CUDA runtime while it unloads (rg_finalize releases them explicitly).
     std::map<int, std::unique_ptr<DeviceContext>>& contexts() {
-      static std::map<int, std::unique_ptr<DeviceContext>> m;
-      return m;
+      static auto* m = new std::map<int, std::unique_ptr<DeviceContext>>();
+      return *m;
     }
   } // namespace
 
@@ -84,6 +86,7 @@ namespace rg {
     RG_TRY(context(&c));
     std::lock_guard<std::mutex> lock(ctx_mutex());
     if (!c->staging) {
+      // on a failed allocation st's destructor releases what was made
       auto st = std::make_unique<HostStaging>();
       for (int b = 0; b < HostStaging::kBuffers; ++b) {
         RG_CUDA_TRY(cudaMalloc(&st->d_stage[b], sizeof(float) * kComps * HostStaging::kChunk));
@@ -97,25 +100,24 @@ namespace rg {
     return RG_OK;
   }
 
+  HostStaging::~HostStaging() {
+    if (copy_stream) {
+      cudaStreamSynchronize(copy_stream);
+      cudaStreamDestroy(copy_stream);
+    }
+    for (int b = 0; b < kBuffers; ++b) {
+      if (consumed[b]) {
+        cudaEventSynchronize(consumed[b]);
+        cudaEventDestroy(consumed[b]);
+      }
+      if (copied[b]) {
+        cudaEventDestroy(copied[b]);
+      }
+      cudaFree(d_stage[b]); // null for a buffer never allocated
+    }
+  }
+
   void free_staging(DeviceContext& c) {
-    if (!c.staging) {
-      return;
-    }
-    HostStaging& st = *c.staging;
-    if (st.copy_stream) {
-      cudaStreamSynchronize(st.copy_stream);
-      cudaStreamDestroy(st.copy_stream);
-    }
-    for (int b = 0; b < HostStaging::kBuffers; ++b) {
-      if (st.consumed[b]) {
-        cudaEventSynchronize(st.consumed[b]);
-        cudaEventDestroy(st.consumed[b]);
-      }
-      if (st.copied[b]) {
-        cudaEventDestroy(st.copied[b]);
-      }
-      cudaFree(st.d_stage[b]);
-    }
     c.staging.reset();
   }
 
