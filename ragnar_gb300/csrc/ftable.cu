@@ -202,14 +202,13 @@ namespace rg {
     RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float2) * kRefEntries));
     RG_CUDA_TRY(cudaMemcpyAsync(t.d_x, t.h_x.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
     const std::vector<float> grids = inner_grids(t.h_x);
-    float*                   d_grids = nullptr;
-    RG_CUDA_TRY(cudaMalloc(&d_grids, sizeof(float) * grids.size()));
-    RG_CUDA_TRY(cudaMemcpyAsync(d_grids, grids.data(), sizeof(float) * grids.size(),
+    ScratchBuffer<float>     d_grids;
+    RG_CUDA_TRY(cudaMalloc(&d_grids.p, sizeof(float) * grids.size()));
+    RG_CUDA_TRY(cudaMemcpyAsync(d_grids.p, grids.data(), sizeof(float) * grids.size(),
                                 cudaMemcpyHostToDevice, s));
-    ffunc_integrand_kernel<<<(n + 3) / 4, 128, 0, s>>>(t.d_x, d_grids, n, t.d_y, 1);
+    ffunc_integrand_kernel<<<(n + 3) / 4, 128, 0, s>>>(t.d_x, d_grids.p, n, t.d_y, 1);
     RG_CUDA_TRY(cudaGetLastError());
     RG_CUDA_TRY(cudaStreamSynchronize(s));
-    RG_CUDA_TRY(cudaFree(d_grids));
     ref_coef_kernel<<<kRefEntries / 256, 256, 0, s>>>(t.d_x, t.d_y, n, t.ln_xmin, t.dln, t.d_coef);
     RG_CUDA_TRY(cudaGetLastError());
     t.h_y.resize(n);
@@ -248,18 +247,17 @@ namespace rg {
   int build_smooth_table(SmoothTable& t, cudaStream_t s) {
     t.ln_xmin = std::log(kSmoothXmin);
     t.dln     = std::log(kSmoothXmax / kSmoothXmin) / kSmoothSegments;
-    double2* nodes = nullptr;
-    RG_CUDA_TRY(cudaMalloc(&nodes, sizeof(double2) * (kSmoothSegments + 1)));
+    ScratchBuffer<double2> nodes;
+    RG_CUDA_TRY(cudaMalloc(&nodes.p, sizeof(double2) * (kSmoothSegments + 1)));
     RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float4) * (kSmoothSegments + 1)));
     RG_CUDA_TRY(cudaMemsetAsync(t.d_coef + kSmoothSegments, 0, sizeof(float4), s));
     smooth_nodes_kernel<<<(kSmoothSegments + 1 + 127) / 128, 128, 0, s>>>(kSmoothSegments + 1,
-                                                                           t.ln_xmin, t.dln, nodes);
+                                                                           t.ln_xmin, t.dln, nodes.p);
     RG_CUDA_TRY(cudaGetLastError());
-    smooth_coef_kernel<<<(kSmoothSegments + 127) / 128, 128, 0, s>>>(nodes, kSmoothSegments, t.dln,
+    smooth_coef_kernel<<<(kSmoothSegments + 127) / 128, 128, 0, s>>>(nodes.p, kSmoothSegments, t.dln,
                                                                      t.d_coef);
     RG_CUDA_TRY(cudaGetLastError());
     RG_CUDA_TRY(cudaStreamSynchronize(s));
-    RG_CUDA_TRY(cudaFree(nodes));
     return RG_OK;
   }
 
@@ -276,17 +274,15 @@ namespace rg {
       RG_CUDA_TRY(cudaMemcpyAsync(hx.data(), x, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
       RG_CUDA_TRY(cudaStreamSynchronize(s));
       const std::vector<float> grids = inner_grids(hx);
-      float*                   d_grids = nullptr;
-      RG_CUDA_TRY(cudaMalloc(&d_grids, sizeof(float) * grids.size()));
-      RG_CUDA_TRY(cudaMemcpyAsync(d_grids, grids.data(), sizeof(float) * grids.size(),
+      ScratchBuffer<float>     d_grids;
+      RG_CUDA_TRY(cudaMalloc(&d_grids.p, sizeof(float) * grids.size()));
+      RG_CUDA_TRY(cudaMemcpyAsync(d_grids.p, grids.data(), sizeof(float) * grids.size(),
                                   cudaMemcpyHostToDevice, s));
-      ffunc_integrand_kernel<<<static_cast<unsigned>((n + 3) / 4), 128, 0, s>>>(x, d_grids, n, y,
+      ffunc_integrand_kernel<<<static_cast<unsigned>((n + 3) / 4), 128, 0, s>>>(x, d_grids.p, n, y,
                                                                                zero_first);
-      const cudaError_t launch = cudaGetLastError();
-      const cudaError_t sync   = cudaStreamSynchronize(s);
-      cudaFree(d_grids);
-      RG_CUDA_TRY(launch);
-      RG_CUDA_TRY(sync);
+      RG_CUDA_TRY(cudaGetLastError());
+      // the host grids and the scratch must outlive the kernel
+      RG_CUDA_TRY(cudaStreamSynchronize(s));
       return RG_OK;
     }
   } // namespace

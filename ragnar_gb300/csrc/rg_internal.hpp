@@ -34,6 +34,16 @@ namespace rg {
     }                                                                                   \
   } while (0)
 
+  // Scratch device buffer freed when it leaves scope (also on an early error return).
+  template <typename T>
+  struct ScratchBuffer {
+    T* p = nullptr;
+    ScratchBuffer() = default;
+    ScratchBuffer(const ScratchBuffer&) = delete;
+    ScratchBuffer& operator=(const ScratchBuffer&) = delete;
+    ~ScratchBuffer() { cudaFree(p); }
+  };
+
   // Particle streams of a spectrum input: u0 u1 u2 e0 e1 e2 b0 b1 b2 w.
   constexpr int kComps = 10;
 
