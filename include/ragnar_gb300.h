@@ -256,7 +256,8 @@ typedef struct rg_fromdist_plan rg_fromdist_plan;
  * runs as one BF16 tensor-core GEMM (tcgen05) over split-precision operands:
  * split_products = 6 (three BF16 terms per operand, ~1e-8 relative per product)
  * or 3 (two terms, ~1e-5 relative).  bins is host (nbins).  Either table mode.
- * Creation builds K, splits it and autotunes the GEMM tile shape (synchronous).
+ * Creation builds K, splits it and autotunes the GEMM tile shape and split-K count
+ * (synchronous).
  * Extension: the reference handles one distribution per call. */
 int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, const float* bins, int32_t nbins,
                             float g_syn, float e_syn_at_g_syn, int32_t table_mode, int32_t split_products,
@@ -282,6 +283,18 @@ int rg_fromdist_plan_config(const rg_fromdist_plan* plan, int32_t* fwd_bn, int32
 /* Overrides the tuned shapes with entries 0..2 of the supported list
  * ((256, 4), (128, 6), (128, 4)); -1 keeps the current choice. */
 int rg_fromdist_plan_set_config(rg_fromdist_plan* plan, int32_t fwd_cfg, int32_t adj_cfg);
+
+/* Split-K range counts of the forward and adjoint GEMMs (1: none): the gamma (or
+ * photon) blocks are cut into that many ranges computed by separate CTAs and
+ * summed in range order (deterministic), which fills the GPU when there are few
+ * output tiles.  Tuned with the tile shape at plan creation.  No reference
+ * counterpart. */
+int rg_fromdist_plan_split_k(const rg_fromdist_plan* plan, int32_t* fwd_split, int32_t* adj_split);
+
+/* Overrides the tuned counts: 1, 2, 4 or 8 and at most the direction's number of
+ * 64-wide k blocks; -1 keeps the current choice.  May allocate the plan's workspace
+ * (synchronous). */
+int rg_fromdist_plan_set_split_k(rg_fromdist_plan* plan, int32_t fwd_split, int32_t adj_split);
 
 /* Copies the FP64 kernel matrix K (nbins x ng) to host memory. */
 int rg_fromdist_kernel_matrix(rg_fromdist_plan* plan, double* K_host);

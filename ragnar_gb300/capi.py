@@ -105,6 +105,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_fromdist_plan_config": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                                     ctypes.POINTER(_i32)],
         "rg_fromdist_plan_set_config": [_vp, _i32, _i32],
+        "rg_fromdist_plan_split_k": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+        "rg_fromdist_plan_set_split_k": [_vp, _i32, _i32],
         "rg_ic_spectrum": [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp],
         "rg_energy_thresholds": [_vp, _i32, _i32, _vp, ctypes.POINTER(_i32)],
         "rg_smooth_table": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
@@ -298,6 +300,15 @@ class FromDistPlan:
 
     def set_config(self, fwd: int = -1, adj: int = -1) -> None:
         check(lib().rg_fromdist_plan_set_config(self.handle, fwd, adj))
+
+    def split_k(self) -> dict:
+        """Autotuned split-K range counts {"fwd": n, "adj": n} (1: no split)."""
+        v = [_i32() for _ in range(2)]
+        check(lib().rg_fromdist_plan_split_k(self.handle, *[ctypes.byref(x) for x in v]))
+        return {"fwd": v[0].value, "adj": v[1].value}
+
+    def set_split_k(self, fwd: int = -1, adj: int = -1) -> None:
+        check(lib().rg_fromdist_plan_set_split_k(self.handle, fwd, adj))
 
     def kernel_matrix(self):
         import numpy as np  # noqa: PLC0415

@@ -174,6 +174,8 @@ namespace rg {
       int          ldc;
       const float* col_scale;  // per output column (nullable)
       unsigned*    status;
+      int          splits;       // K split into this many gamma-block ranges (blockIdx.z); 1: none
+      int64_t      split_stride; // elements between the C slices of consecutive ranges
     };
 
     // Warps 2..9 turn the FP32 left operand into BF16 terms in shared memory.
@@ -198,7 +200,10 @@ namespace rg {
 
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
-      const int nk = g.nstore * g.kpt; // ring: gamma block outer, right term inner
+      // this CTA's gamma blocks [gb0, gb0 + nloc) (all of them unless K is split)
+      const int gb0  = static_cast<int>(static_cast<int64_t>(blockIdx.z) * g.kpt / g.splits);
+      const int nloc = static_cast<int>(static_cast<int64_t>(blockIdx.z + 1) * g.kpt / g.splits) - gb0;
+      const int nk   = g.nstore * nloc; // ring: gamma block outer, right term inner
 
       if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -234,23 +239,23 @@ namespace rg {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
-          // right term r of gamma block gb
-          const int gb = kb / g.nstore, r = kb - gb * g.nstore;
+          // right term r of gamma block gb0 + i
+          const int i = kb / g.nstore, r = kb - i * g.nstore;
           mbar_arrive_expect_tx(&b_full[s], kBytesB);
-          tma_load_2d(sB + s * kBytesB, &tmB, (r * g.kpt + gb) * kBK, n0, &b_full[s]);
+          tma_load_2d(sB + s * kBytesB, &tmB, (r * g.kpt + gb0 + i) * kBK, n0, &b_full[s]);
         }
       } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer -------------------------------------------------------------------
         bool     ok      = true;
         uint32_t started = 0; // bit a: accumulator a holds a partial sum
-        for (int gb = 0; gb < g.kpt && ok; ++gb) {
-          const int ab = gb & 1;
-          if (!mbar_wait_bounded(&a_full[ab], static_cast<uint32_t>(gb >> 1) & 1u)) {
+        for (int i = 0; i < nloc && ok; ++i) {
+          const int ab = i & 1;
+          if (!mbar_wait_bounded(&a_full[ab], static_cast<uint32_t>(i >> 1) & 1u)) {
             atomicOr(g.status, kDevGemmTimeout);
             break;
           }
           for (int r = 0; r < g.nstore; ++r) {
-            const int      kb = gb * g.nstore + r;
+            const int      kb = i * g.nstore + r;
             const int      s  = kb % kStages;
             const uint32_t ph = static_cast<uint32_t>(kb / kStages) & 1u;
             if (!mbar_wait_bounded(&b_full[s], ph)) {
@@ -280,10 +285,10 @@ namespace rg {
         // ---- converters: FP32 left operand -> BF16 terms, 128-byte swizzled -----------------
         const int  ct  = threadIdx.x - 64;
         const bool vec = (g.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(g.left) & 15) == 0;
-        for (int gb = 0; gb < g.kpt; ++gb) {
-          const int ab = gb & 1;
-          if (gb >= 2 &&
-              !__all_sync(0xffffffffu, mbar_wait_bounded(&a_empty[ab], static_cast<uint32_t>((gb - 2) >> 1) & 1u))) {
+        for (int i = 0; i < nloc; ++i) {
+          const int gb = gb0 + i, ab = i & 1;
+          if (i >= 2 &&
+              !__all_sync(0xffffffffu, mbar_wait_bounded(&a_empty[ab], static_cast<uint32_t>((i - 2) >> 1) & 1u))) {
             if (lane == 0) {
               atomicOr(g.status, kDevGemmTimeout);
             }
@@ -357,15 +362,22 @@ namespace rg {
         }
       }
       tc_fence_after();
-      if (done && nk > 0 && warp < 4) {
+      if (done && warp < 4) {
         const int  row = m0 + warp * 32 + lane;
         const bool two = g.nprod > 1; // accumulator 1 was written
 #pragma unroll 1
         for (int c = 0; c < kBN / 32; ++c) {
           float          v[32];
           const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
-          tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
-          if (two) {
+          if (nk == 0) { // an empty gamma range (more ranges than gamma blocks) adds zero
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              v[j] = 0.0f;
+            }
+          } else {
+            tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
+          }
+          if (two && nk > 0) {
             float w[32];
             tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(kBN + c * 32), w);
 #pragma unroll
@@ -375,7 +387,7 @@ namespace rg {
           }
           const int col0 = n0 + c * 32;
           if (row < g.M && col0 < g.N) {
-            float* dst = g.C + static_cast<int64_t>(row) * g.ldc + col0;
+            float* dst = g.C + blockIdx.z * g.split_stride + static_cast<int64_t>(row) * g.ldc + col0;
             if (g.col_scale) {
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
@@ -403,6 +415,22 @@ namespace rg {
       if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(kTmemCols)
                      : "memory");
+      }
+    }
+
+    // Split-K reduction: C[r, c] = sum over ranges z = 0, 1, ... (in that order) of the
+    // range's slice; deterministic.
+    __global__ void splitk_reduce_kernel(const float* __restrict__ ws, int splits, int64_t stride, int M, int N,
+                                         float* __restrict__ C, int ldc) {
+      const int64_t n = static_cast<int64_t>(M) * N;
+      for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+           i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float t = ws[i];
+        for (int z = 1; z < splits; ++z) {
+          t = __fadd_rn(t, ws[z * stride + i]);
+        }
+        const int64_t r = i / N, c = i - r * N;
+        C[r * ldc + c] = t;
       }
     }
 
@@ -515,7 +543,7 @@ namespace rg {
                                          static_cast<int>(gemm_smem(cfg, 3))));
         configured = true;
       }
-      const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM);
+      const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, g.splits);
       gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg, g.nstore), s>>>(tB, g);
       RG_CUDA_TRY(cudaGetLastError());
       return RG_OK;
@@ -566,17 +594,73 @@ struct rg_fromdist_plan {
   unsigned*      d_status = nullptr;
   CUtensorMap    tB[2], tBT[2]; // right operands with box height 256 and 128
   int            cfg_fwd = 0, cfg_adj = 0; // autotuned tile shapes
+  int            split_fwd = 1, split_adj = 1; // autotuned split-K range counts
+  float*         d_ws   = nullptr; // split-K slices (split x max_dist x N floats)
+  size_t         ws_cap = 0;       // floats
 };
 
 namespace rg {
 
   namespace {
 
-    // Times every tile shape on the plan's own GEMM (max_dist rows, zero left
-    // operand) and returns the fastest; results are cached per device and shape.
-    int tune_gemm(rg_fromdist_plan* pl, bool adjoint, int* best_cfg) {
-      static std::mutex                            mu;
-      static std::map<std::vector<int>, int>       cache;
+    constexpr int kSplits[]   = { 1, 2, 4, 8 }; // split-K range counts the autotuner tries
+    constexpr int kNumSplits  = 4;
+
+    // A split-K range count is usable if every range holds a gamma block.
+    bool split_ok(int split, int kpt) {
+      return split >= 1 && split <= kpt;
+    }
+
+    int ensure_workspace(rg_fromdist_plan* pl, size_t floats) {
+      if (floats <= pl->ws_cap) {
+        return RG_OK;
+      }
+      RG_CUDA_TRY(cudaDeviceSynchronize()); // the old slices may still be read
+      cudaFree(pl->d_ws);
+      pl->d_ws   = nullptr;
+      pl->ws_cap = 0;
+      RG_CUDA_TRY(cudaMalloc(&pl->d_ws, sizeof(float) * floats));
+      pl->ws_cap = floats;
+      return RG_OK;
+    }
+
+    // One GEMM: C = g.C (row stride g.ldc).  With split > 1 the gamma blocks are cut into
+    // `split` ranges (blockIdx.z) whose products land in the plan's workspace slices, then
+    // summed in range order into C.  The workspace must already hold split x M x N floats.
+    int run_gemm(rg_fromdist_plan* pl, int cfg, int split, const CUtensorMap& tB, GemmArgs g, cudaStream_t s) {
+      g.splits       = 1;
+      g.split_stride = 0;
+      if (split <= 1 || g.M <= 0 || g.N <= 0) {
+        return launch_gemm(cfg, tB, g, s);
+      }
+      if (!split_ok(split, g.kpt)) {
+        return set_error(RG_ERR_ARGUMENT, "split-K range count above the number of gamma blocks");
+      }
+      const int64_t n = static_cast<int64_t>(g.M) * g.N;
+      if (static_cast<size_t>(split) * static_cast<size_t>(n) > pl->ws_cap) {
+        return set_error(RG_ERR_ARGUMENT, "split-K workspace smaller than the request (ndist above max_dist?)");
+      }
+      float*    out = g.C;
+      const int ldc = g.ldc;
+      g.C            = pl->d_ws;
+      g.ldc          = g.N;
+      g.splits       = split;
+      g.split_stride = n;
+      RG_TRY(launch_gemm(cfg, tB, g, s));
+      DeviceContext* ctx = nullptr;
+      RG_TRY(context(&ctx));
+      const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, static_cast<int64_t>(ctx->sms) * 8));
+      splitk_reduce_kernel<<<blocks, 256, 0, s>>>(pl->d_ws, split, n, g.M, g.N, out, ldc);
+      RG_CUDA_TRY(cudaGetLastError());
+      return RG_OK;
+    }
+
+    // Times every tile shape and split-K range count on the plan's own GEMM (max_dist
+    // rows, zero left operand) and returns the fastest; results are cached per device
+    // and shape.
+    int tune_gemm(rg_fromdist_plan* pl, bool adjoint, int* best_cfg, int* best_split) {
+      static std::mutex                                   mu;
+      static std::map<std::vector<int>, std::pair<int, int>> cache;
       int dev = 0;
       RG_CUDA_TRY(cudaGetDevice(&dev));
       GemmArgs g {};
@@ -596,8 +680,9 @@ namespace rg {
         std::lock_guard<std::mutex> lock(mu);
         const auto it = cache.find(key);
         if (it != cache.end()) {
-          *best_cfg = it->second;
-          return RG_OK;
+          *best_cfg   = it->second.first;
+          *best_split = it->second.second;
+          return ensure_workspace(pl, static_cast<size_t>(*best_split) * g.M * g.N);
         }
       }
       float*      C  = nullptr;
@@ -624,33 +709,54 @@ namespace rg {
       }
       g.C        = C;
       g.left     = L;
-      int   best = 0;
+      int maxsplit = 1;
+      for (int si = 0; si < kNumSplits; ++si) {
+        if (split_ok(kSplits[si], g.kpt)) {
+          maxsplit = std::max(maxsplit, kSplits[si]);
+        }
+      }
+      {
+        const int st = ensure_workspace(pl, static_cast<size_t>(maxsplit) * g.M * g.N);
+        if (st != RG_OK) {
+          return fail(st);
+        }
+      }
+      int   best = 0, best_sp = 1;
       float best_ms = 0.0f;
+      bool  first   = true;
       for (int cfg = 0; cfg < kNumConfigs; ++cfg) {
         const CUtensorMap& tB = adjoint ? pl->tBT[box_index(cfg)] : pl->tB[box_index(cfg)];
-        for (int r = 0; r < 2; ++r) {
-          const int st = launch_gemm(cfg, tB, g, nullptr);
-          if (st != RG_OK) {
-            return fail(st);
+        for (int si = 0; si < kNumSplits; ++si) {
+          const int split = kSplits[si];
+          if (!split_ok(split, g.kpt)) {
+            continue;
           }
-        }
-        e = cudaEventRecord(e0, nullptr);
-        for (int r = 0; r < 5 && e == cudaSuccess; ++r) {
-          const int st = launch_gemm(cfg, tB, g, nullptr);
-          if (st != RG_OK) {
-            return fail(st);
+          for (int r = 0; r < 2; ++r) {
+            const int st = run_gemm(pl, cfg, split, tB, g, nullptr);
+            if (st != RG_OK) {
+              return fail(st);
+            }
           }
-        }
-        if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float ms = 0.0f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e != cudaSuccess) {
-          return fail(cuda_error(e, "GEMM autotuning"));
-        }
-        if (cfg == 0 || ms < best_ms) {
-          best    = cfg;
-          best_ms = ms;
+          e = cudaEventRecord(e0, nullptr);
+          for (int r = 0; r < 5 && e == cudaSuccess; ++r) {
+            const int st = run_gemm(pl, cfg, split, tB, g, nullptr);
+            if (st != RG_OK) {
+              return fail(st);
+            }
+          }
+          if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          float ms = 0.0f;
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          if (e != cudaSuccess) {
+            return fail(cuda_error(e, "GEMM autotuning"));
+          }
+          if (first || ms < best_ms) {
+            best    = cfg;
+            best_sp = split;
+            best_ms = ms;
+            first   = false;
+          }
         }
       }
       unsigned st = 0;
@@ -663,8 +769,9 @@ namespace rg {
         return set_error(RG_ERR_TIMEOUT, "a bounded wait in the tensor-core GEMM gave up during autotuning");
       }
       std::lock_guard<std::mutex> lock(mu);
-      cache[key] = best;
-      *best_cfg  = best;
+      cache[key]  = { best, best_sp };
+      *best_cfg   = best;
+      *best_split = best_sp;
       return RG_OK;
     }
 
@@ -777,8 +884,8 @@ int rg_fromdist_plan_create(const float* gbeta, int32_t ng, int32_t log_spaced, 
     st = rg::encode_tiled(&pl->tB[b], pl->d_B, kf, nbins, box);
     if (st == RG_OK) st = rg::encode_tiled(&pl->tBT[b], pl->d_BT, ka, ng, box);
   }
-  if (st == RG_OK) st = rg::tune_gemm(pl.get(), false, &pl->cfg_fwd);
-  if (st == RG_OK) st = rg::tune_gemm(pl.get(), true, &pl->cfg_adj);
+  if (st == RG_OK) st = rg::tune_gemm(pl.get(), false, &pl->cfg_fwd, &pl->split_fwd);
+  if (st == RG_OK) st = rg::tune_gemm(pl.get(), true, &pl->cfg_adj, &pl->split_adj);
   if (st != RG_OK) {
     return fail(st);
   }
@@ -797,6 +904,7 @@ int rg_fromdist_plan_destroy(rg_fromdist_plan* pl) {
   cudaFree(pl->d_B);
   cudaFree(pl->d_BT);
   cudaFree(pl->d_status);
+  cudaFree(pl->d_ws);
   delete pl;
   return RG_OK;
 }
@@ -822,7 +930,8 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
   g.ldc        = pl->nbins;
   g.col_scale  = pl->d_ebins;
   g.status     = pl->d_status;
-  return rg::launch_gemm(pl->cfg_fwd, pl->tB[rg::box_index(pl->cfg_fwd)], g, static_cast<cudaStream_t>(stream));
+  return rg::run_gemm(pl, pl->cfg_fwd, pl->split_fwd, pl->tB[rg::box_index(pl->cfg_fwd)], g,
+                      static_cast<cudaStream_t>(stream));
 }
 
 int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndist, float* grad_f, void* stream) {
@@ -847,7 +956,8 @@ int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndi
   g.ldc        = pl->ng;
   g.col_scale  = nullptr;
   g.status     = pl->d_status;
-  return rg::launch_gemm(pl->cfg_adj, pl->tBT[rg::box_index(pl->cfg_adj)], g, static_cast<cudaStream_t>(stream));
+  return rg::run_gemm(pl, pl->cfg_adj, pl->split_adj, pl->tBT[rg::box_index(pl->cfg_adj)], g,
+                      static_cast<cudaStream_t>(stream));
 }
 
 int rg_fromdist_plan_check(rg_fromdist_plan* pl, void* stream) {
@@ -883,6 +993,41 @@ int rg_fromdist_plan_set_config(rg_fromdist_plan* pl, int32_t fwd_cfg, int32_t a
   }
   if (fwd_cfg >= 0) pl->cfg_fwd = fwd_cfg;
   if (adj_cfg >= 0) pl->cfg_adj = adj_cfg;
+  return RG_OK;
+}
+
+int rg_fromdist_plan_split_k(const rg_fromdist_plan* pl, int32_t* fwd_split, int32_t* adj_split) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  if (fwd_split) *fwd_split = pl->split_fwd;
+  if (adj_split) *adj_split = pl->split_adj;
+  return RG_OK;
+}
+
+int rg_fromdist_plan_set_split_k(rg_fromdist_plan* pl, int32_t fwd_split, int32_t adj_split) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  const int kf = pl->gpad / rg::kBK, ka = pl->epad / rg::kBK;
+  auto listed  = [](int v) {
+    for (int si = 0; si < rg::kNumSplits; ++si) {
+      if (rg::kSplits[si] == v) return true;
+    }
+    return false;
+  };
+  if ((fwd_split >= 0 && (!listed(fwd_split) || !rg::split_ok(fwd_split, kf))) ||
+      (adj_split >= 0 && (!listed(adj_split) || !rg::split_ok(adj_split, ka)))) {
+    return rg::set_error(RG_ERR_ARGUMENT,
+                         "rg_fromdist_plan_set_split_k: counts are 1, 2, 4 or 8 and at most the gamma blocks");
+  }
+  const int    f    = fwd_split >= 0 ? fwd_split : pl->split_fwd;
+  const int    a    = adj_split >= 0 ? adj_split : pl->split_adj;
+  const size_t need = std::max(static_cast<size_t>(f) * pl->max_dist * pl->nbins,
+                               static_cast<size_t>(a) * pl->max_dist * pl->ng);
+  RG_TRY(rg::ensure_workspace(pl, need));
+  pl->split_fwd = f;
+  pl->split_adj = a;
   return RG_OK;
 }
 

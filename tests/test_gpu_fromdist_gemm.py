@@ -197,6 +197,33 @@ def test_every_tile_shape(gpu, oracle_lib, table, cfg):
         plan.set_config(3, 0)
 
 
+@pytest.mark.parametrize("split", [1, 2, 4, 8])
+def test_every_split_k(gpu, oracle_lib, table, split):
+    """Split-K forced to each count the autotuner may pick: the ranges' products summed in
+    range order match the FP64 oracle (forward) and K^T (adjoint), and reruns are
+    bit-identical."""
+    gb = oracle_lib.logspace(1.0, 1e5, 600)   # 10 k blocks of 64
+    bins = oracle_lib.logspace(0.01, 1e11, 520)  # 9 k blocks for the adjoint
+    f = _dists(gb, 130, seed=70 + split)
+    plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=130)
+    assert plan.split_k()["fwd"] in (1, 2, 4, 8) and plan.split_k()["adj"] in (1, 2, 4, 8)
+    plan.set_split_k(split, split)
+    assert plan.split_k() == {"fwd": split, "adj": split}
+    S = _run(plan, f, gpu)
+    S64 = oracle_lib.sync_from_dist_f64(gb, f, True, bins, 1.0, 1.0, table)
+    assert _rows_max_rel(S, S64) <= SPECTRUM_RTOL
+    assert np.array_equal(S, _run(plan, f, gpu))
+    gS = np.random.default_rng(split).standard_normal((130, 520)).astype(np.float32)
+    gf = torch.empty((130, 600), device=gpu)
+    plan.adjoint(torch.from_numpy(gS).to(gpu), gf)
+    plan.check()
+    want = (gS.astype(np.float64) * bins.astype(np.float64)[None, :]) @ plan.kernel_matrix()
+    assert np.max(np.abs(gf.cpu().numpy() - want) / np.max(np.abs(want), axis=1, keepdims=True)) < 1e-5
+    for bad in ((3, -1), (16, -1), (-1, 16)):
+        with pytest.raises(capi.RgError, match="counts are 1, 2, 4 or 8"):
+            plan.set_split_k(*bad)
+
+
 def test_forward_and_adjoint_replay_from_cuda_graph(gpu, oracle_lib):
     """The split + GEMM forward and the transpose-GEMM adjoint make no host
     synchronisation or allocation, so a training step can be captured once and replayed."""
