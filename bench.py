@@ -696,6 +696,7 @@ def fromdist_gemm_case(torch, capi, device, peak_bf16):
     for terms in (6, 3):
         plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=nd, split_products=terms)
         tuned = plan.config()
+        tuned_split = plan.split_k()
         shapes = {}
         for cfg, (bn, stages) in enumerate([(256, 4), (128, 6), (128, 4)]):
             plan.set_config(cfg, -1)
@@ -712,7 +713,8 @@ def fromdist_gemm_case(torch, capi, device, peak_bf16):
         res[f"bf16x{terms}"] = {
             "evals_per_s": nd * ng * ne / t, "ms": t * 1e3, "bf16_tflops": flops / t / 1e12,
             "frac_of_bf16_peak": flops / t / 1e12 / peak_bf16, "max_rel_err_vs_fp64": err,
-            "autotuned_tile": {"fwd": list(tuned["fwd"]), "adj": list(tuned["adj"])}, "tile_timings": shapes}
+            "autotuned_tile": {"fwd": list(tuned["fwd"]), "adj": list(tuned["adj"])},
+            "autotuned_split_k": tuned_split, "tile_timings": shapes}
         plan.close()
     res["peak_bf16_tflops"] = peak_bf16
     return res
