@@ -25,12 +25,15 @@
 // tiles, double-buffered per 64-gamma block: no split kernel and no BF16 copy in
 // HBM.  The k loop runs gamma block outer, right term inner, and every product of
 // a resident right term runs before its ring stage is released, so each converted
-// left tile and each streamed right tile serves every product that uses it.  One thread issues tcgen05.mma (M 128, N =
-// tile width, K 16) and commits each ring stage back to the producer and each
-// left buffer back to the converters; after the last commit warps 0..3 read both
-// accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and write
-// (acc0 + acc1) * col_scale.  Every mbarrier wait is bounded; a wait that gives up
-// records the status word, and the CTA still frees its tensor memory.
+// left tile and each streamed right tile serves every product that uses it.  One
+// thread issues tcgen05.mma (M 128, N = tile width, K 16) and commits each ring
+// stage back to the producer and each left buffer back to the converters; after
+// the last commit warps 0..7 read both accumulators with tcgen05.ld (warp w owns
+// TMEM lanes 32(w%4)..+31, half w/4 of the columns), scale them by col_scale,
+// write them into 128-byte-swizzled 32 x 128 boxes in the ring's shared memory,
+// and one thread stores the boxes with TMA tensor stores (direct stores when the
+// output is not 16-byte aligned).  Every mbarrier wait is bounded; a wait that
+// gives up records the status word, and the CTA still frees its tensor memory.
 #include "rg_common.cuh"
 #include "rg_internal.hpp"
 
@@ -74,6 +77,21 @@ namespace rg {
           "r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
+    }
+
+    // Tensor store of one 32-column x 128-row FP32 box (128-byte swizzled in shared memory)
+    // at (x, y, z) of a 3-D map; out-of-range rows and columns are not written.
+    __device__ __forceinline__ void tma_store_3d(const CUtensorMap* tm, const void* src, int x, int y, int z) {
+      asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<uint64_t>(tm)),
+                   "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
+                   : "memory");
+    }
+
+    // Commits the issued tensor stores and waits until they have completed.
+    __device__ __forceinline__ void tma_store_commit_and_wait() {
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
 
     // Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle
@@ -139,6 +157,37 @@ namespace rg {
       }
     }
 
+    // Both accumulators' 32 columns at once: two loads, one wait.
+    __device__ __forceinline__ void tmem_ld32x2(uint32_t ta, uint32_t tb, float (&v)[32], float (&w)[32]) {
+      uint32_t r[32], q[32];
+      asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+        "[%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(ta));
+      asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+        "[%32];"
+        : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]), "=r"(q[5]), "=r"(q[6]), "=r"(q[7]),
+          "=r"(q[8]), "=r"(q[9]), "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]),
+          "=r"(q[15]), "=r"(q[16]), "=r"(q[17]), "=r"(q[18]), "=r"(q[19]), "=r"(q[20]), "=r"(q[21]),
+          "=r"(q[22]), "=r"(q[23]), "=r"(q[24]), "=r"(q[25]), "=r"(q[26]), "=r"(q[27]), "=r"(q[28]),
+          "=r"(q[29]), "=r"(q[30]), "=r"(q[31])
+        : "r"(tb));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        v[i] = __uint_as_float(r[i]);
+        w[i] = __uint_as_float(q[i]);
+      }
+    }
+
     // Splits v into BF16 terms h, m, l (each the rounding of the remainder).
     __device__ __forceinline__ void split3(double v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
       h         = __double2bfloat16(v);
@@ -176,6 +225,7 @@ namespace rg {
       unsigned*    status;
       int          splits;       // K split into this many gamma-block ranges (blockIdx.z); 1: none
       int64_t      split_stride; // elements between the C slices of consecutive ranges
+      int          c_tma;        // 1: the epilogue stores C tiles with TMA through tmC
     };
 
     // Warps 2..9 turn the FP32 left operand into BF16 terms in shared memory.
@@ -185,7 +235,8 @@ namespace rg {
 
     template <int kBN, int kStages>
     __global__ void __launch_bounds__(kGemmThreads, 1)
-      gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmB, const __grid_constant__ GemmArgs g) {
+      gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmC,
+                          const __grid_constant__ GemmArgs g) {
       constexpr uint32_t kBytesB   = kBN * kBK * 2;
       constexpr uint32_t kTmemCols = 2 * kBN; // two accumulators
       constexpr uint32_t kIdesc    = idesc<kBN>();
@@ -362,38 +413,59 @@ namespace rg {
         }
       }
       tc_fence_after();
-      if (done && warp < 4) {
-        const int  row = m0 + warp * 32 + lane;
-        const bool two = g.nprod > 1; // accumulator 1 was written
+      // the tile's output column scales (1 when there are none), staged in the left operand's
+      // shared memory, which no MMA reads any more
+      float* s_scale = reinterpret_cast<float*>(sA);
+      if (done) {
+        for (int i = threadIdx.x; i < kBN; i += kGemmThreads) {
+          const int col = n0 + i;
+          s_scale[i]    = !g.col_scale ? 1.0f : (col < g.N ? __ldg(g.col_scale + col) : 0.0f);
+        }
+      }
+      __syncthreads();
+      // warps 0..7: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) for half w / 4 of the columns
+      if (done && warp < 8) {
+        const int      q         = warp & 3, half = warp >> 2;
+        const int      r         = q * 32 + lane; // row within the tile
+        const int      row       = m0 + r;
+        const bool     two       = g.nprod > 1;   // accumulator 1 was written
+        const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
+        constexpr int  kHalf     = kBN / 64;      // 32-column chunks per half
 #pragma unroll 1
-        for (int c = 0; c < kBN / 32; ++c) {
-          float          v[32];
-          const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+        for (int c = half * kHalf; c < (half + 1) * kHalf; ++c) {
+          float v[32];
           if (nk == 0) { // an empty gamma range (more ranges than gamma blocks) adds zero
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               v[j] = 0.0f;
             }
-          } else {
-            tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
-          }
-          if (two && nk > 0) {
+          } else if (two) {
             float w[32];
-            tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(kBN + c * 32), w);
+            tmem_ld32x2(tmem_d + lane_base + static_cast<uint32_t>(c * 32),
+                        tmem_d + lane_base + static_cast<uint32_t>(kBN + c * 32), v, w);
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               v[j] += w[j];
             }
+          } else {
+            tmem_ld32(tmem_d + lane_base + static_cast<uint32_t>(c * 32), v);
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            v[j] *= s_scale[c * 32 + j];
           }
           const int col0 = n0 + c * 32;
-          if (row < g.M && col0 < g.N) {
-            float* dst = g.C + blockIdx.z * g.split_stride + static_cast<int64_t>(row) * g.ldc + col0;
-            if (g.col_scale) {
+          if (g.c_tma) {
+            // box c of the ring's shared memory: 128 rows of 128 bytes, 16-byte piece p of
+            // row r at piece p ^ (r % 8) (the map's 128-byte swizzle; conflict-free stores)
+            unsigned char* box = sB + c * (kBM * 128);
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                v[j] *= (col0 + j < g.N) ? __ldg(g.col_scale + col0 + j) : 0.0f;
-              }
+            for (int p4 = 0; p4 < 8; ++p4) {
+              *reinterpret_cast<float4*>(box + r * 128 + ((p4 ^ (r & 7)) << 4)) =
+                make_float4(v[4 * p4], v[4 * p4 + 1], v[4 * p4 + 2], v[4 * p4 + 3]);
             }
+          } else if (row < g.M && col0 < g.N) {
+            float* dst = g.C + blockIdx.z * g.split_stride + static_cast<int64_t>(row) * g.ldc + col0;
             if (col0 + 32 <= g.N && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
 #pragma unroll
               for (int j = 0; j < 32; j += 4) {
@@ -408,6 +480,19 @@ namespace rg {
               }
             }
           }
+        }
+      }
+      if (g.c_tma) {
+        // generic-proxy writes of the boxes -> visible to the tensor store; one thread stores
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (done && threadIdx.x == 0) {
+          for (int c = 0; c < kBN / 32; ++c) {
+            if (n0 + c * 32 < g.N) {
+              tma_store_3d(&tmC, sB + c * (kBM * 128), n0 + c * 32, m0, static_cast<int>(blockIdx.z));
+            }
+          }
+          tma_store_commit_and_wait(); // the boxes are read and C written before the CTA exits
         }
       }
       tc_fence_before();
@@ -528,6 +613,36 @@ namespace rg {
       return RG_OK;
     }
 
+    // Tensor map of the output for the epilogue's tensor stores: FP32 [ranges][M][N] with row
+    // stride ldc and range stride `stride` (elements), boxes of 32 columns x 128 rows in the
+    // 128-byte swizzle.  Returns false (the epilogue then stores directly) when the base or
+    // the strides are not 16-byte multiples or the driver refuses the map.
+    bool encode_c_map(CUtensorMap* tm, float* base, int N, int M, int ranges, int ldc, int64_t stride) {
+      static EncodeTiledFn fn = nullptr;
+      if (!fn) {
+        void*                           p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+              cudaSuccess ||
+            !p || q != cudaDriverEntryPointSuccess) {
+          cudaGetLastError();
+          return false;
+        }
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+      }
+      if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ldc & 3) != 0 || (stride & 3) != 0) {
+        return false;
+      }
+      const cuuint64_t dims[3]    = { static_cast<cuuint64_t>(N), static_cast<cuuint64_t>(M),
+                                      static_cast<cuuint64_t>(ranges) };
+      const cuuint64_t strides[2] = { static_cast<cuuint64_t>(ldc) * 4, static_cast<cuuint64_t>(stride) * 4 };
+      const cuuint32_t box[3]     = { 32, static_cast<cuuint32_t>(kBM), 1 };
+      const cuuint32_t estr[3]    = { 1, 1, 1 };
+      return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+
     // right-operand ring + two buffers of the left operand's BF16 term tiles + alignment slack
     size_t gemm_smem(int cfg, int nstore) {
       return static_cast<size_t>(kConfigs[cfg].stages) * kConfigs[cfg].bn * kBK * 2 +
@@ -535,7 +650,7 @@ namespace rg {
     }
 
     template <int BN, int STAGES>
-    int launch_gemm_t(int cfg, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+    int launch_gemm_t(int cfg, const CUtensorMap& tB, const CUtensorMap& tC, const GemmArgs& g, cudaStream_t s) {
       static bool configured = false;
       if (!configured) {
         RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, STAGES>,
@@ -544,23 +659,27 @@ namespace rg {
         configured = true;
       }
       const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, g.splits);
-      gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg, g.nstore), s>>>(tB, g);
+      gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg, g.nstore), s>>>(tB, tC, g);
       RG_CUDA_TRY(cudaGetLastError());
       return RG_OK;
     }
 
-    // tB is the right operand's tensor map whose box height is the config's bn.
-    int launch_gemm(int cfg, const CUtensorMap& tB, const GemmArgs& g, cudaStream_t s) {
+    // tB is the right operand's tensor map whose box height is the config's bn; the output's
+    // map is made here (g.C, g.ldc, g.splits ranges g.split_stride apart).
+    int launch_gemm(int cfg, const CUtensorMap& tB, GemmArgs g, cudaStream_t s) {
       if (g.M <= 0 || g.N <= 0) {
         return RG_OK;
       }
+      CUtensorMap tC {};
+      const int64_t stride = g.splits > 1 ? g.split_stride : static_cast<int64_t>(g.M) * g.ldc;
+      g.c_tma = encode_c_map(&tC, g.C, g.N, g.M, g.splits, g.ldc, stride) ? 1 : 0;
       switch (cfg) {
         case 0:
-          return launch_gemm_t<kConfigs[0].bn, kConfigs[0].stages>(0, tB, g, s);
+          return launch_gemm_t<kConfigs[0].bn, kConfigs[0].stages>(0, tB, tC, g, s);
         case 1:
-          return launch_gemm_t<kConfigs[1].bn, kConfigs[1].stages>(1, tB, g, s);
+          return launch_gemm_t<kConfigs[1].bn, kConfigs[1].stages>(1, tB, tC, g, s);
         case 2:
-          return launch_gemm_t<kConfigs[2].bn, kConfigs[2].stages>(2, tB, g, s);
+          return launch_gemm_t<kConfigs[2].bn, kConfigs[2].stages>(2, tB, tC, g, s);
         default:
           return set_error(RG_ERR_ARGUMENT, "unknown GEMM configuration");
       }
