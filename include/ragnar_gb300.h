@@ -8,6 +8,12 @@
  * failure on the calling thread.  Unless stated otherwise, a call only enqueues
  * work on `stream` and returns without synchronising.
  *
+ * Threads: the library's own state (device contexts, tables, the host staging
+ * pipeline, caches) is guarded and may be used from several threads.  A plan
+ * (rg_spectrum_plan, rg_fromdist_plan) holds scratch that its runs reuse: calls on
+ * one plan must be ordered on one stream (or externally synchronised), and two
+ * plans are needed for work that overlaps.
+ *
  * Each declaration cites the reference interface it replaces (file:line in the
  * reference tree, paths under src/).
  */
