@@ -286,15 +286,11 @@ namespace rg {
     template <int K, int MODE>
     cudaError_t launch_adjoint_k(const FusedParams& fp, const AdjExtra& x, int grid, size_t smem,
                                  cudaStream_t s) {
-      static bool configured = false;
-      if (!configured) {
-        const cudaError_t e =
-          cudaFuncSetAttribute(adjoint_kernel<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(adjoint_smem(MODE, kSmoothSegments, kComps)));
-        if (e != cudaSuccess) {
-          return e;
-        }
-        configured = true;
+      static std::atomic<uint64_t> configured { 0 };
+      const cudaError_t            e = ensure_max_dynamic_smem(
+        adjoint_kernel<K, MODE>, static_cast<int>(adjoint_smem(MODE, kSmoothSegments, kComps)), configured);
+      if (e != cudaSuccess) {
+        return e;
       }
       adjoint_kernel<K, MODE><<<grid, kThreads, smem, s>>>(fp, x);
       return cudaGetLastError();

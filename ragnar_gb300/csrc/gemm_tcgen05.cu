@@ -589,16 +589,26 @@ namespace rg {
                                        CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
                                        CUtensorMapFloatOOBfill);
 
-    int encode_tiled(CUtensorMap* tm, void* base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
-      static EncodeTiledFn fn = nullptr;
-      if (!fn) {
+    // cuTensorMapEncodeTiled from the driver (looked up once, thread-safe), or null.
+    EncodeTiledFn encode_fn() {
+      static const EncodeTiledFn fn = []() -> EncodeTiledFn {
         void*                           p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        RG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-        if (!p || q != cudaDriverEntryPointSuccess) {
-          return set_error(RG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+              cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+          cudaGetLastError();
+          return nullptr;
         }
-        fn = reinterpret_cast<EncodeTiledFn>(p);
+        return reinterpret_cast<EncodeTiledFn>(p);
+      }();
+      return fn;
+    }
+
+    int encode_tiled(CUtensorMap* tm, void* base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
+      const EncodeTiledFn fn = encode_fn();
+      if (!fn) {
+        return set_error(RG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
       }
       const cuuint64_t dims[2]    = { cols, rows };
       const cuuint64_t strides[1] = { cols * 2 };
@@ -618,17 +628,9 @@ namespace rg {
     // 128-byte swizzle.  Returns false (the epilogue then stores directly) when the base or
     // the strides are not 16-byte multiples or the driver refuses the map.
     bool encode_c_map(CUtensorMap* tm, float* base, int N, int M, int ranges, int ldc, int64_t stride) {
-      static EncodeTiledFn fn = nullptr;
+      const EncodeTiledFn fn = encode_fn();
       if (!fn) {
-        void*                           p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-              cudaSuccess ||
-            !p || q != cudaDriverEntryPointSuccess) {
-          cudaGetLastError();
-          return false;
-        }
-        fn = reinterpret_cast<EncodeTiledFn>(p);
+        return false;
       }
       if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ldc & 3) != 0 || (stride & 3) != 0) {
         return false;
@@ -651,13 +653,9 @@ namespace rg {
 
     template <int BN, int STAGES>
     int launch_gemm_t(int cfg, const CUtensorMap& tB, const CUtensorMap& tC, const GemmArgs& g, cudaStream_t s) {
-      static bool configured = false;
-      if (!configured) {
-        RG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, STAGES>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(gemm_smem(cfg, 3))));
-        configured = true;
-      }
+      static std::atomic<uint64_t> configured { 0 };
+      RG_CUDA_TRY(ensure_max_dynamic_smem(gemm_bf16_tn_kernel<BN, STAGES>, static_cast<int>(gemm_smem(cfg, 3)),
+                                          configured));
       const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, g.splits);
       gemm_bf16_tn_kernel<BN, STAGES><<<grid, kGemmThreads, gemm_smem(cfg, g.nstore), s>>>(tB, tC, g);
       RG_CUDA_TRY(cudaGetLastError());

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <memory>
 #include <mutex>
@@ -33,6 +34,26 @@ namespace rg {
       return rg_s_;                                                                     \
     }                                                                                   \
   } while (0)
+
+  // Raises a kernel's dynamic shared-memory limit to `bytes` once per device (the
+  // attribute is per device; `done` keeps one bit per device ordinal below 64).
+  template <typename Kernel>
+  cudaError_t ensure_max_dynamic_smem(Kernel* kernel, int bytes, std::atomic<uint64_t>& done) {
+    int               dev = 0;
+    const cudaError_t e0  = cudaGetDevice(&dev);
+    if (e0 != cudaSuccess) {
+      return e0;
+    }
+    const uint64_t bit = dev < 64 ? (uint64_t(1) << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) {
+      return cudaSuccess;
+    }
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) {
+      done.fetch_or(bit, std::memory_order_release);
+    }
+    return e;
+  }
 
   // Scratch device buffer freed when it leaves scope (also on an early error return).
   template <typename T>

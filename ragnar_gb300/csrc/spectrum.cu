@@ -523,15 +523,11 @@ namespace rg {
 
     template <int K, int MODE>
     cudaError_t launch_fused_k(const FusedParams& fp, dim3 grid, size_t smem, cudaStream_t s) {
-      static bool configured = false;
-      if (!configured) {
-        const cudaError_t e =
-          cudaFuncSetAttribute(fused_spectrum_kernel<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)));
-        if (e != cudaSuccess) {
-          return e;
-        }
-        configured = true;
+      static std::atomic<uint64_t> configured { 0 };
+      const cudaError_t            e = ensure_max_dynamic_smem(
+        fused_spectrum_kernel<K, MODE>, static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)), configured);
+      if (e != cudaSuccess) {
+        return e;
       }
       fused_spectrum_kernel<K, MODE><<<grid, kThreads, smem, s>>>(fp);
       return cudaGetLastError();
