@@ -37,8 +37,9 @@ namespace rg {
 
     constexpr int kIcThreads = 256;
     constexpr int kIcWarps   = kIcThreads / 32;
-    constexpr int kIcSlice   = 512;
+    constexpr int kIcSlice   = 512; // the widest slice of IC bins (K = 16 rows of 32 per lane)
     constexpr int kIcSChunk  = 64; // soft photons per work item
+    constexpr int kIcMaxRows = 16; // rows of 32 IC bins per lane (the slice width is rows x 32)
 
     struct IcParams {
       const float* gb;      // ng gamma (gamma beta) bins
@@ -52,7 +53,8 @@ namespace rg {
       const float* eic;     // ne IC photon energies
       int          ne;
       int          nslices;
-      double*      partials; // [grid][nslices][kIcSlice]: one row per block
+      int          slice_w;  // IC bins per slice: K x 32
+      double*      partials; // [grid][nslices][slice_w]: one row per block
     };
 
     // inv4es, ws and the smallest positive inv4es (positive floats order like their bit
@@ -84,7 +86,7 @@ namespace rg {
       // this lane's IC energy of row k (0 for padding and for invalid bins); reloaded
       // where needed (per item) instead of held in registers
       auto energy = [&](int k) -> float {
-        const int   bin = slice * kIcSlice + k * 32 + lane;
+        const int   bin = slice * (K * 32) + k * 32 + lane;
         const float e   = bin < p.ne ? __ldg(p.eic + bin) : 0.0f;
         return (e > 0.0f && isfinite(e)) ? e : 0.0f;
       };
@@ -159,15 +161,15 @@ namespace rg {
       __shared__ double red[kIcWarps * kIcSlice];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        red[warp * kIcSlice + k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
+        red[warp * (K * 32) + k * 32 + lane] = static_cast<double>(hi[k]) + static_cast<double>(lo[k]);
       }
       __syncthreads();
-      double* dst = p.partials + (b * p.nslices + slice) * kIcSlice;
+      double* dst = p.partials + (b * p.nslices + slice) * (K * 32);
       for (int j = threadIdx.x; j < K * 32; j += kIcThreads) {
         double t = 0.0;
 #pragma unroll
         for (int w = 0; w < kIcWarps; ++w) {
-          t += red[w * kIcSlice + j];
+          t += red[w * (K * 32) + j];
         }
         dst[j] = t;
       }
@@ -175,16 +177,17 @@ namespace rg {
 
     // out[e] = sum over blocks (fixed order) of the partial rows; 32 bins x 32 row groups.
     __global__ void __launch_bounds__(1024)
-      ic_reduce_kernel(const double* __restrict__ partials, int grid, int nslices, int ne, float* __restrict__ out) {
+      ic_reduce_kernel(const double* __restrict__ partials, int grid, int nslices, int slice_w, int ne,
+                       float* __restrict__ out) {
       __shared__ double part[32][33];
       const int bin = blockIdx.x * 32 + threadIdx.x, ty = threadIdx.y;
       double    sum = 0.0;
       if (bin < ne) {
-        const int slice = bin / kIcSlice, j = bin % kIcSlice;
+        const int slice = bin / slice_w, j = bin % slice_w;
         // unrolled so that several rows' loads are in flight (the adds stay in row order)
 #pragma unroll 8
         for (int r = ty; r < grid; r += 32) {
-          sum += partials[(static_cast<int64_t>(r) * nslices + slice) * kIcSlice + j];
+          sum += partials[(static_cast<int64_t>(r) * nslices + slice) * slice_w + j];
         }
       }
       part[ty][threadIdx.x] = sum;
@@ -240,8 +243,9 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   }
   rg::DeviceContext* ctx = nullptr;
   RG_TRY(rg::context(&ctx));
-  const int     nslices = (ne + rg::kIcSlice - 1) / rg::kIcSlice;
-  const int     K       = std::min(16, (std::min(ne, rg::kIcSlice) + 31) / 32);
+  const int     K       = std::min(rg::kIcMaxRows, (std::min(ne, rg::kIcSlice) + 31) / 32);
+  const int     slice_w = K * 32;
+  const int     nslices = (ne + slice_w - 1) / slice_w;
   const int64_t items   = static_cast<int64_t>(ng) * ((ns + rg::kIcSChunk - 1) / rg::kIcSChunk);
   const int     grid    = static_cast<int>(std::max<int64_t>(
     1, std::min<int64_t>(2 * ctx->sms, (items + rg::kIcWarps - 1) / rg::kIcWarps)));
@@ -249,7 +253,7 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   const size_t off_ws   = 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_min  = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_part = off_min + 256;
-  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * rg::kIcSlice;
+  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * slice_w;
   unsigned char* buf    = nullptr;
   RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
   rg::IcParams p {};
@@ -263,6 +267,7 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   p.eic        = eic;
   p.ne         = ne;
   p.nslices    = nslices;
+  p.slice_w    = slice_w;
   p.partials   = reinterpret_cast<double*>(buf + off_part);
   p.inv4es_min = reinterpret_cast<float*>(buf + off_min);
   // the minimum slot starts at 0x7f7f7f7f (3.4e38, above any 1 / (4 e_s) of a positive float)
@@ -275,7 +280,8 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   }
   if (e == cudaSuccess) e = rg::launch_ic(K, p, dim3(grid, nslices), s);
   if (e == cudaSuccess) {
-    rg::ic_reduce_kernel<<<dim3((ne + 31) / 32), dim3(32, 32), 0, s>>>(p.partials, grid, nslices, ne, out);
+    rg::ic_reduce_kernel<<<dim3((ne + 31) / 32), dim3(32, 32), 0, s>>>(p.partials, grid, nslices, slice_w, ne,
+                                                                        out);
     e = cudaGetLastError();
   }
   const cudaError_t ef = cudaFreeAsync(buf, s);
