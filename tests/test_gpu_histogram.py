@@ -136,3 +136,31 @@ def test_threshold_cache_eviction(gpu, oracle_lib):
             h, c = gpu_hist(P["ux"], P["uy"], P["uz"], bins, True, True, gpu)
             _, h64, cnt = oracle_lib.energy_distribution(P["ux"], P["uy"], P["uz"], bins, True, True)
             np.testing.assert_array_equal(c, cnt)
+
+
+def test_more_than_2_pow_31_particles(gpu):
+    """2^31 + 12345 particles (26 GB of u): 64-bit indexing; every particle is counted once
+    and two halves add up to the whole."""
+    n = (1 << 31) + 12345
+    gen = torch.Generator(device=gpu).manual_seed(11)
+    u = [torch.rand(n, device=gpu, generator=gen) * 20 - 10 for _ in range(3)]
+    bins = np.logspace(-2, 3, 100).astype(np.float32)
+
+    def run(lo, hi):
+        hist = torch.empty(100, device=gpu)
+        counts = torch.empty(100, dtype=torch.int64, device=gpu)
+        capi.check(capi.lib().rg_energy_distribution(u[0][lo:].data_ptr(), u[1][lo:].data_ptr(),
+                                                     u[2][lo:].data_ptr(), hi - lo, bins.ctypes.data, 100,
+                                                     1, 1, hist.data_ptr(), counts.data_ptr(), 0))
+        torch.cuda.synchronize()
+        return hist.double().cpu().numpy(), counts.cpu().numpy()
+
+    h, c = run(0, n)
+    h1, c1 = run(0, 1 << 30)
+    h2, c2 = run(1 << 30, n)
+    del u
+    torch.cuda.empty_cache()
+    assert int(c.sum()) == n
+    np.testing.assert_array_equal(c, c1 + c2)
+    m = h > 0
+    assert np.max(np.abs(h1[m] + h2[m] - h[m]) / h[m]) < 1e-6

@@ -331,3 +331,28 @@ def test_host_streaming_pageable_memory(gpu, oracle_lib, table):
     plan.check()
     assert torch.equal(out, out2)
     assert max_rel(out.cpu().numpy(), oracle_lib.sync_spectrum_f64(P, bins, 1.0, 1.0, 1.0, table)) <= SPECTRUM_RTOL
+
+
+def test_more_than_2_pow_31_particles(gpu):
+    """2^31 + 777 particles (u and B each one 8.6 GB stream used for all three components):
+    64-bit particle and item indexing; one launch equals the sum of a two-segment batch."""
+    n = (1 << 31) + 777
+    gen = torch.Generator(device=gpu).manual_seed(12)
+    u = torch.rand(n, device=gpu, generator=gen) * 30 + 0.5
+    b = torch.rand(n, device=gpu, generator=gen) + 0.2
+    prt = capi.particles([u, u, u], b=[b, -b, b], n=n)
+    bins = np.logspace(-2, 6, 32).astype(np.float32)
+    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
+    plan.reserve(2)
+    full = torch.empty(32, device=gpu)
+    plan.run(prt, full)
+    plan.check()
+    split = torch.empty((2, 32), device=gpu)
+    offs = torch.tensor([0, (1 << 30) + 3, n], dtype=torch.int64, device=gpu)
+    plan.run_batched(prt, offs, 2, split)
+    plan.check()
+    f, s = full.double().cpu().numpy(), split.double().sum(0).cpu().numpy()
+    del u, b
+    torch.cuda.empty_cache()
+    assert np.all(np.isfinite(f)) and f.max() > 0
+    assert max_rel(s, f) < 1e-6
