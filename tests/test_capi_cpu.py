@@ -124,6 +124,15 @@ def test_module_exposes_reference_api():
                      "is_allocated", "nactive", "nalloc", "label", "energyDistribution", "X", "U",
                      "E", "B", "__len__", "__repr__"):
             assert hasattr(c, meth), (cls, meth)
+    for cls, meths in (("Array1D_i", ("as_array", "extent", "head", "__repr__")),
+                       ("Array1D_f", ("as_array", "extent", "head", "__repr__")),
+                       ("Array1D_d", ("as_array", "extent", "head", "__repr__")),
+                       ("Bins", ("log_spaced", "unit")),
+                       ("TabulatedDistribution", ("extent", "log_spaced", "EnergyBins", "F")),
+                       ("PlawGenerator", ("compute",)), ("BrokenPlawGenerator", ("compute",)),
+                       ("DeltaGenerator", ("compute",))):
+        for meth in meths:
+            assert hasattr(getattr(rg, cls), meth), (cls, meth)
     assert rg.EnergyUnits.mec2 == "mec2" and rg.EnergyUnits.mpc2 == "mpc2"
     p = rg.Particles_3D("electrons")
     assert p.label() == "electrons" and not p.is_allocated() and len(p) == 0
