@@ -198,12 +198,14 @@ def test_every_tile_shape(gpu, oracle_lib, table, cfg):
 
 
 @pytest.mark.parametrize("split", [1, 2, 4, 8])
-def test_every_split_k(gpu, oracle_lib, table, split):
+@pytest.mark.parametrize("ng,nbins", [(600, 520), (601, 522)])
+def test_every_split_k(gpu, oracle_lib, table, split, ng, nbins):
     """Split-K forced to each count the autotuner may pick: the ranges' products summed in
     range order match the FP64 oracle (forward) and K^T (adjoint), and reruns are
-    bit-identical."""
-    gb = oracle_lib.logspace(1.0, 1e5, 600)   # 10 k blocks of 64
-    bins = oracle_lib.logspace(0.01, 1e11, 520)  # 9 k blocks for the adjoint
+    bit-identical; row lengths that are multiples of 4 take the tensor-store epilogue, the
+    others the direct stores."""
+    gb = oracle_lib.logspace(1.0, 1e5, ng)   # 10 k blocks of 64
+    bins = oracle_lib.logspace(0.01, 1e11, nbins)  # 9 k blocks for the adjoint
     f = _dists(gb, 130, seed=70 + split)
     plan = capi.FromDistPlan(gb, True, bins, 1.0, 1.0, max_dist=130)
     assert plan.split_k()["fwd"] in (1, 2, 4, 8) and plan.split_k()["adj"] in (1, 2, 4, 8)
@@ -213,8 +215,8 @@ def test_every_split_k(gpu, oracle_lib, table, split):
     S64 = oracle_lib.sync_from_dist_f64(gb, f, True, bins, 1.0, 1.0, table)
     assert _rows_max_rel(S, S64) <= SPECTRUM_RTOL
     assert np.array_equal(S, _run(plan, f, gpu))
-    gS = np.random.default_rng(split).standard_normal((130, 520)).astype(np.float32)
-    gf = torch.empty((130, 600), device=gpu)
+    gS = np.random.default_rng(split).standard_normal((130, nbins)).astype(np.float32)
+    gf = torch.empty((130, ng), device=gpu)
     plan.adjoint(torch.from_numpy(gS).to(gpu), gf)
     plan.check()
     want = (gS.astype(np.float64) * bins.astype(np.float64)[None, :]) @ plan.kernel_matrix()
