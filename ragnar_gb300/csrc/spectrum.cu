@@ -65,7 +65,7 @@ namespace rg {
     // block at a point where no warp reads the (q, A) buffers that serve as scratch.
     template <int K>
     __device__ __forceinline__ void flush_block(float (&hi)[K], float (&lo)[K], double* scratch, double* dst,
-                                                int tid) {
+                                                int tid, bool accumulate) {
       const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
       for (int k0 = 0; k0 < K; k0 += kFlushRows) {
@@ -84,7 +84,8 @@ namespace rg {
           for (int w = 0; w < kWarps; ++w) {
             t += scratch[(r * kWarps + w) * 32 + lane];
           }
-          dst[(k0 + r) * 32 + lane] = t;
+          double* d = dst + (k0 + r) * 32 + lane;
+          *d        = accumulate ? *d + t : t;
         }
         __syncthreads();
       }
@@ -193,7 +194,8 @@ namespace rg {
           // block-uniform (info[st] is shared); every warp is past the previous item's
           // evaluation (the barrier above), so the (q, A) buffers are free
           if (cur_seg >= 0) {
-            flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid);
+            flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid,
+                           p.accumulate != 0);
           }
           cur_seg = I.seg;
         }
@@ -252,7 +254,8 @@ namespace rg {
       }
       if (cur_seg >= 0) {
         __syncthreads(); // every warp is done reading the last item's (q, A)
-        flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid);
+        flush_block<K>(hi, lo, reinterpret_cast<double*>(qa), block_partial(p, b, cur_seg, slice), tid,
+                       p.accumulate != 0);
       }
     }
 
@@ -328,7 +331,6 @@ namespace rg {
       const uint8_t*  valid;
       const unsigned* status;
       float*          out;   // nseg x nbins
-      double*         acc64; // when set: acc64 += result in FP64 instead of writing out
     };
 
     // Block (32 bins x kReduceRows row groups): row group y sums the block partial
@@ -402,20 +404,7 @@ namespace rg {
         }
         result = t * static_cast<double>(r.ebins[bin]);
       }
-      const int64_t o = static_cast<int64_t>(s) * r.nbins + bin;
-      if (r.acc64) {
-        r.acc64[o] += result;
-      } else {
-        r.out[o] = __double2float_rn(result);
-      }
-    }
-
-    __global__ void finalize_acc_kernel(const double* __restrict__ acc, int n, const unsigned* status,
-                                        float* __restrict__ out) {
-      const int i = blockIdx.x * blockDim.x + threadIdx.x;
-      if (i < n) {
-        out[i] = (*status != kDevOk) ? __int_as_float(0x7fc00000) : __double2float_rn(acc[i]);
-      }
+      r.out[static_cast<int64_t>(s) * r.nbins + bin] = __double2float_rn(result);
     }
 
     // ---- plain baseline kernel ------------------------------------------------------
@@ -797,7 +786,6 @@ namespace rg {
     rp.valid       = valid;
     rp.status      = status;
     rp.out         = out;
-    rp.acc64       = nullptr;
     reduce_partials_kernel<<<dim3((nbins + 31) / 32, 1), dim3(32, kReduceRows), 0, s>>>(rp);
     RG_CUDA_TRY(cudaGetLastError());
     return RG_OK;
@@ -811,18 +799,43 @@ namespace rg {
 
   namespace {
 
+    // The reduction of a launch's partial rows into `out` (nseg x nbins): `grid` blocks over
+    // the items of n_single particles (or of the segments of d_prefix).
+    int reduce_rows(rg_spectrum_plan* pl, const int64_t* d_prefix, int64_t n_single, int grid, int nseg,
+                    float* out, cudaStream_t s) {
+      ReduceParams rp {};
+      rp.partials    = pl->d_partials;
+      rp.item_prefix = d_prefix;
+      rp.n_single    = n_single;
+      rp.grid        = grid;
+      rp.nslices     = pl->nslices;
+      rp.nseg        = nseg;
+      rp.nbins       = pl->nbins;
+      rp.ebins       = pl->d_ebins;
+      rp.valid       = pl->d_valid;
+      rp.status      = pl->d_status;
+      rp.out         = out;
+      dim3 rgrid((pl->nbins + 31) / 32, nseg);
+      reduce_partials_kernel<<<rgrid, dim3(32, kReduceRows), 0, s>>>(rp);
+      RG_CUDA_TRY(cudaGetLastError());
+      return RG_OK;
+    }
+
+    // Blocks of the fused kernel over a single segment of n particles.
+    int single_segment_grid(const rg_spectrum_plan* pl, int64_t n) {
+      const int64_t items = (n + kChunk - 1) / kChunk;
+      return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(items, pl->grid)));
+    }
+
     // Launches fused + reduce.  `d_off` (device, nseg + 1) may be null for a
-    // single segment [0, n_single).  With `acc64` the spectra are added in FP64
-    // to acc64 (nseg x nbins) instead of being written to `out`.
+    // single segment [0, n_single).
     int run_fused(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off,
-                  int64_t n_single, int nseg, float* out, cudaStream_t s, double* acc64 = nullptr) {
+                  int64_t n_single, int nseg, float* out, cudaStream_t s) {
       if (nseg <= 0 || pl->nbins == 0) {
         return RG_OK;
       }
       if (pl->zero) {
-        if (!acc64) {
-          RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins * nseg, s));
-        }
+        RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins * nseg, s));
         return RG_OK;
       }
       RG_TRY(plan_reserve(pl, nseg));
@@ -834,31 +847,27 @@ namespace rg {
       FusedParams fp;
       const int   nslots = fill_params(pl, comp, d_off, d_prefix, n_single, nseg, fp);
       // a single segment with fewer items than blocks uses fewer blocks
-      int G = pl->grid;
-      if (!d_off) {
-        const int64_t items = (n_single + kChunk - 1) / kChunk;
-        G = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(items, pl->grid)));
-      }
+      const int G = d_off ? pl->grid : single_segment_grid(pl, n_single);
       const bool any = d_off ? true : n_single > 0;
       if (any) {
         RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(pl->table_mode, kSmoothSegments, nslots), s));
       }
-      ReduceParams rp {};
-      rp.partials    = pl->d_partials;
-      rp.item_prefix = d_prefix;
-      rp.n_single    = n_single;
-      rp.grid        = G;
-      rp.nslices     = pl->nslices;
-      rp.nseg        = nseg;
-      rp.nbins       = pl->nbins;
-      rp.ebins       = pl->d_ebins;
-      rp.valid       = pl->d_valid;
-      rp.status      = pl->d_status;
-      rp.out         = out;
-      rp.acc64       = acc64;
-      dim3 rgrid((pl->nbins + 31) / 32, nseg);
-      reduce_partials_kernel<<<rgrid, dim3(32, kReduceRows), 0, s>>>(rp);
-      RG_CUDA_TRY(cudaGetLastError());
+      return reduce_rows(pl, d_prefix, n_single, G, nseg, out, s);
+    }
+
+    // One chunk of a host-resident run (a single segment of n particles): the blocks write
+    // their partial rows (first chunk) or add to them (later chunks, no larger than the
+    // first); the rows are reduced once after the last chunk.
+    int run_fused_chunk(rg_spectrum_plan* pl, const float* const comp[kComps], int64_t n, bool accumulate,
+                        cudaStream_t s) {
+      RG_TRY(plan_reserve(pl, 1));
+      FusedParams fp;
+      const int   nslots = fill_params(pl, comp, nullptr, nullptr, n, 1, fp);
+      fp.accumulate      = accumulate ? 1 : 0;
+      if (n > 0) {
+        RG_TRY(timed_launch(pl, fp, dim3(single_segment_grid(pl, n), pl->nslices),
+                            fused_smem(pl->table_mode, kSmoothSegments, nslots), s));
+      }
       return RG_OK;
     }
 
@@ -930,7 +939,6 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_partials);
   cudaFree(pl->d_prefix);
   cudaFree(pl->d_plain_acc);
-  cudaFree(pl->d_acc64);
   for (auto* v : { &pl->ev_used, &pl->ev_free }) {
     for (auto& e : *v) {
       cudaEventDestroy(e.first);
@@ -1037,19 +1045,20 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
     return RG_OK;
   }
   auto s = static_cast<cudaStream_t>(stream);
-  if (!pl->d_acc64) {
-    RG_CUDA_TRY(cudaMalloc(&pl->d_acc64, sizeof(double) * pl->nbins));
+  if (pl->zero) {
+    RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins, s));
+    return RG_OK;
   }
-  // 2^22-particle chunks, double-buffered (each chunk costs a kernel tail and a reduction,
-  // so chunks are kept large; 2^21-particle chunks and a third buffer were measured slower
-  // or no faster)
+  // 2^22-particle chunks, double-buffered (each chunk costs a kernel launch and tail, so
+  // chunks are kept large; 2^21-particle chunks and a third buffer were measured slower or
+  // no faster).  The chunks' blocks accumulate into their partial rows and one reduction
+  // at the end writes the spectrum.
   rg::HostStaging* st = nullptr;
   RG_TRY(rg::host_staging(&st));
   constexpr int64_t kStageChunk = rg::HostStaging::kChunk;
   constexpr int     kBuffers    = rg::HostStaging::kBuffers;
   const float*      host[rg::kComps];
   rg::particle_comps(p, host);
-  RG_CUDA_TRY(cudaMemsetAsync(pl->d_acc64, 0, sizeof(double) * pl->nbins, s));
   // consumed[b] was last recorded after the kernel that read staging buffer b (in an
   // earlier call on this device, by any plan, or never): the first copies of this call
   // wait for exactly that, so they overlap the tail of the previous call's kernels
@@ -1070,13 +1079,12 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
     }
     RG_CUDA_TRY(cudaEventRecord(st->copied[b], st->copy_stream));
     RG_CUDA_TRY(cudaStreamWaitEvent(s, st->copied[b], 0));
-    RG_TRY(rg::run_fused(pl, dev, nullptr, m, 1, out, s, pl->d_acc64));
+    RG_TRY(rg::run_fused_chunk(pl, dev, m, a > 0, s));
     RG_CUDA_TRY(cudaEventRecord(st->consumed[b], s));
   }
-  rg::finalize_acc_kernel<<<(pl->nbins + 255) / 256, 256, 0, s>>>(pl->d_acc64, pl->nbins, pl->d_status,
-                                                                  out);
-  RG_CUDA_TRY(cudaGetLastError());
-  return RG_OK;
+  // the rows the chunks accumulated: as many blocks as the first (largest) chunk used
+  const int64_t first = std::min(kStageChunk, n);
+  return rg::reduce_rows(pl, nullptr, first, rg::single_segment_grid(pl, first), 1, out, s);
 }
 
 int rg_spectrum_run_plain(const rg_spectrum_plan* cplan, const rg_particles* p, float* out,

@@ -53,6 +53,7 @@ namespace rg {
     int            hseg;
     int            frac;
     double*        partials;     // [(grid + nseg) * nslices * kSliceBins]
+    int            accumulate;   // 1: a block adds its sums to its partial row (chunked runs)
     int            nslices;
     unsigned*      status;
     // Always 0 (zero-initialised with the struct).  The kernel builds an integer

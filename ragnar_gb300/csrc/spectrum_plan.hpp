@@ -42,9 +42,6 @@ struct rg_spectrum_plan {
   // kernel timing (events bracketing each fused launch)
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
-  // host-resident runs: FP64 spectrum accumulated over the staged chunks (the staging
-  // buffers and copy stream belong to the device, rg::HostStaging)
-  double*      d_acc64     = nullptr;
 };
 
 namespace rg {
