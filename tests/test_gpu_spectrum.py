@@ -356,3 +356,17 @@ def test_more_than_2_pow_31_particles(gpu):
     torch.cuda.empty_cache()
     assert np.all(np.isfinite(f)) and f.max() > 0
     assert max_rel(s, f) < 1e-6
+
+
+def test_nan_particles_add_nothing(gpu, oracle_lib, table):
+    """A NaN momentum or field gives a NaN peak energy, which the reference's e_peak > 0
+    test skips (synchrotron.hpp:162); such particles add nothing here either."""
+    n = 3000
+    P = particles(n, seed=15, bfield="iso")
+    P["ux"][:100] = np.nan
+    P["bz"][100:200] = np.nan
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    got = gpu_spectrum(P, bins, gpu)
+    assert np.all(np.isfinite(got))
+    only = oracle_lib.sync_spectrum_f64({k: v[200:] for k, v in P.items()}, bins, 1.0, 1.0, 1.0, table)
+    assert max_rel(got, only) <= SPECTRUM_RTOL
