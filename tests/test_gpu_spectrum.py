@@ -370,3 +370,42 @@ def test_nan_particles_add_nothing(gpu, oracle_lib, table):
     assert np.all(np.isfinite(got))
     only = oracle_lib.sync_spectrum_f64({k: v[200:] for k, v in P.items()}, bins, 1.0, 1.0, 1.0, table)
     assert max_rel(got, only) <= SPECTRUM_RTOL
+
+
+def test_host_streaming_from_two_threads(gpu, oracle_lib):
+    """Two host threads, each with its own plan and stream, stream host-resident particles
+    through the device's shared staging buffers at the same time; each result equals the
+    same call made alone."""
+    import threading  # noqa: PLC0415
+
+    bins = oracle_lib.logspace(1e-4, 1e9, 256)
+    sets = [particles((1 << 22) + 1000 * i, seed=60 + i, bfield="iso", weights=True) for i in range(2)]
+    hosts = [host_particles(P) for P in sets]
+    plans = [capi.SpectrumPlan(bins, 1.0, 1.0, 1.0), capi.SpectrumPlan(bins, 1.0, 1.0, 0.5)]
+    alone = []
+    for i in range(2):
+        o = torch.empty(256, device=gpu)
+        plans[i].run_host(hosts[i][1], o)
+        plans[i].check()
+        alone.append(o.cpu())
+    outs = [torch.empty(256, device=gpu) for _ in range(2)]
+    streams = [torch.cuda.Stream(gpu) for _ in range(2)]
+    errors = []
+
+    def worker(i):
+        try:
+            for _ in range(3):
+                plans[i].run_host(hosts[i][1], outs[i], streams[i].cuda_stream)
+            streams[i].synchronize()
+        except Exception as e:  # noqa: BLE001
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    for i in range(2):
+        plans[i].check(streams[i].cuda_stream)
+        assert torch.equal(outs[i].cpu(), alone[i])
