@@ -309,6 +309,15 @@ def traffic_per_particle():
     return None
 
 
+def wavefronts_per_eval():
+    """Shared-memory wavefronts per eval of the fused kernel from the committed ncu summary."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        m = re.search(r"shared_wavefronts_per_eval:\s*([0-9.eE+-]+)", open(path).read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np  # noqa: PLC0415
     import torch  # noqa: PLC0415
@@ -389,6 +398,15 @@ def run_ours(args, rank, world, local_rank):
                       f"timed region (issue slots; no measured FP32 peak is available)",
         "traffic": None if tpp is None else tpp * evals_per_launch / NBINS,
     }
+    wpe = wavefronts_per_eval()
+    if wpe:
+        # the other limit the kernel runs against: the shared-memory data path (one
+        # wavefront per SM-clock) at the table-lookup wavefronts per eval ncu measured
+        lsu_peak = sms * clk * 1e6 / wpe
+        roofline["secondary"] = {
+            "bound": "shared-memory wavefronts", "achieved": evals_per_launch / (kern_ms / 1e3),
+            "peak": lsu_peak, "unit": "evals/s", "frac": evals_per_launch / (kern_ms / 1e3) / lsu_peak,
+            "basis": f"{sms} SMs x {clk:.0f} MHz / {wpe} wavefronts per eval (ncu, committed summary)"}
 
     result = {
         "metric": METRIC, "value": world * evals_per_step / t_step, "unit": UNIT, "n_gpus": world,
