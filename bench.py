@@ -56,7 +56,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram)")
+                    help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram, "
+                         "IC, the drop-in module calls)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "spectrum200", "smooth", "gemm", "histogram", "ic"],
@@ -419,6 +420,7 @@ def run_ours(args, rank, world, local_rank):
     extra = {"spectra_finite": spectra_ok}
     if rank == 0 and not args.no_extras:
         extra["energy_distribution_dump"] = guarded(histogram_case, torch, capi, device, comps, NSPECIES * n_per)
+        extra["dropin_module_3.3e7"] = guarded(dropin_module_case, torch, comps, n_per)
     # e2e: host-resident pinned inputs through the C ABI, copies inside the timed region
     if not args.no_e2e:
         host = [torch.empty(c.numel(), dtype=torch.float32, pin_memory=True) for c in comps]
@@ -845,6 +847,51 @@ def adam_fit_case(torch, capi, device, steps=200):
             "fwd_max_rel_err_vs_fp64": float(np.max(np.abs(Sg[mm] - S64[mm]) / S64[mm])),
             "grad_max_err_vs_fp64_rel_to_row_max": float(np.max(np.abs(gg - g64) /
                                                                 np.max(np.abs(g64), axis=1, keepdims=True)))}
+
+
+def dropin_module_case(torch, comps, n, reps=3):
+    """The reference-facing Python module on one dump-scale species, each call blocking as in
+    the reference: Particles_3D.fromArrays from numpy (pageable host memory, allocation plus
+    one host-to-device copy per component, in place of the reference's element-wise host
+    loops), SynchrotronSpectrum_3D(...).as_array() and energyDistribution(Logbins(...))."""
+    import ragnar_gb300 as rg  # noqa: PLC0415
+
+    rg.SetVerbose(False)
+    rg.Initialize()
+    keys = ("U1", "U2", "U3", "B1", "B2", "B3")
+    host = {k: comps[i][:n].cpu().numpy() for i, k in enumerate(keys)}
+    bins = rg.Logbins(BIN_LO, BIN_HI, NBINS, rg.EnergyUnits.mec2)
+    ebins = rg.Logbins(1e-2, 1e3, 200)
+
+    def wall(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    held = {}
+
+    def ingest():
+        held.pop("p", None)
+        p = rg.Particles_3D("e-")
+        p.fromArrays(host)
+        held["p"] = p
+
+    t_in = wall(ingest)
+    prt = held["p"]
+    t_sp = wall(lambda: rg.SynchrotronSpectrum_3D(prt, bins, 1.0, 1.0, 1.0).as_array())
+    t_h = wall(lambda: prt.energyDistribution(ebins))
+    nbytes = 4 * len(keys) * n
+    return {"particles": n, "timing": f"median of {reps} blocking calls (host wall clock)",
+            "fromArrays_ms": t_in * 1e3, "fromArrays_gbs": nbytes / t_in / 1e9,
+            "fromArrays_bytes": nbytes,
+            "SynchrotronSpectrum_ms": t_sp * 1e3, "SynchrotronSpectrum_evals_per_s": n * NBINS / t_sp,
+            "energyDistribution_ms": t_h * 1e3, "energyDistribution_particles_per_s": n / t_h}
 
 
 def ic_case(torch, capi, device, clk_mhz=2070.0):
