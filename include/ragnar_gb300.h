@@ -144,6 +144,14 @@ int rg_spectrum_plan_reserve(rg_spectrum_plan* plan, int32_t max_segments);
  * (synchrotron.cpp:142) as the point where errors surface. */
 int rg_spectrum_plan_check(rg_spectrum_plan* plan, void* stream);
 
+/* Failure-path self-test (no reference counterpart).  Enqueues one block that
+ * waits on a shared-memory barrier phase that nothing completes, bounded by
+ * `polls` polls (1 .. 2^22); the wait gives up and records the status a fused run
+ * records when a particle-stream copy never lands, so the next
+ * rg_spectrum_plan_check returns RG_ERR_TIMEOUT.  No fault, trap or unbounded
+ * wait is involved and the context stays usable. */
+int rg_spectrum_plan_probe_stage_timeout(rg_spectrum_plan* plan, uint32_t polls, void* stream);
+
 /* The fused forward: out[b] = e_b * sum_p w_p chiR_p F(e_b / e_peak_p) for the
  * particles in `p` (sync::Kernel<D>::operator(), synchrotron.hpp:145-172, summed
  * as SynchrotronSpectrum<D> does).  `out` is nbins device floats. */

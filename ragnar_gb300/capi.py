@@ -79,6 +79,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_plan_destroy": [_vp],
         "rg_spectrum_plan_reserve": [_vp, _i32],
         "rg_spectrum_plan_check": [_vp, _vp],
+        "rg_spectrum_plan_probe_stage_timeout": [_vp, ctypes.c_uint32, _vp],
         "rg_spectrum_run": [_vp, ctypes.POINTER(Particles), _vp, _vp],
         "rg_spectrum_run_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp],
         "rg_spectrum_run_plain": [_vp, ctypes.POINTER(Particles), _vp, _vp],
@@ -233,6 +234,10 @@ class SpectrumPlan:
 
     def check(self, stream: int = 0) -> None:
         check(lib().rg_spectrum_plan_check(self.handle, stream))
+
+    def probe_stage_timeout(self, polls: int, stream: int = 0) -> None:
+        """Records a stage-wait timeout through a bounded wait that nothing completes."""
+        check(lib().rg_spectrum_plan_probe_stage_timeout(self.handle, polls, stream))
 
     def close(self) -> None:
         if getattr(self, "handle", None):

@@ -71,8 +71,9 @@ namespace rg {
   }
 
   // Bounded wait for phase `parity` of `bar`.  Returns false if it gave up.
-  __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (unsigned it = 0; it < kWaitLimit; ++it) {
+  __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                    unsigned limit = kWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it) {
       if (mbar_try_wait(bar, parity)) {
         return true;
       }

@@ -505,6 +505,27 @@ namespace rg {
       }
     }
 
+    // The failure path of the stage wait, taken on purpose without a fault: the
+    // barrier expects two arrivals and gets one, so its phase never completes, every
+    // thread's wait gives up after `polls` polls and the block records the status the
+    // fused kernel records when a particle-stream copy does not land.  No copy is in
+    // flight, so nothing is left to drain.
+    __global__ void __launch_bounds__(64) stage_wait_probe_kernel(unsigned* status, unsigned polls) {
+      __shared__ __align__(8) uint64_t bar;
+      if (threadIdx.x == 0) {
+        mbar_init(&bar, 2);
+        fence_mbar_init();
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        mbar_arrive(&bar);
+      }
+      const bool ok = mbar_wait_bounded(&bar, 0u, polls);
+      if (!__syncthreads_and(ok) && threadIdx.x == 0) {
+        atomicOr(status, kDevTimeoutStage);
+      }
+    }
+
     size_t fused_smem(int mode, int hseg, int nslots) {
       const size_t tab = (mode == kModeRef) ? sizeof(float2) * kRefEntries : sizeof(float4) * (hseg + 1);
       return tab + sizeof(int2) * 2 * kChunk + sizeof(float) * 2 * nslots * kChunkPad;
@@ -978,6 +999,18 @@ int rg_spectrum_plan_check(rg_spectrum_plan* pl, void* stream) {
     return rg::set_error(RG_ERR_TIMEOUT, "a bounded wait on the GPU gave up (status " + std::to_string(st) +
                                            "); results are invalid");
   }
+  return RG_OK;
+}
+
+int rg_spectrum_plan_probe_stage_timeout(rg_spectrum_plan* pl, uint32_t polls, void* stream) {
+  if (!pl) {
+    return rg::set_error(RG_ERR_ARGUMENT, "null plan");
+  }
+  if (polls == 0 || polls > rg::kWaitLimit) {
+    return rg::set_error(RG_ERR_ARGUMENT, "polls must be in [1, " + std::to_string(rg::kWaitLimit) + "]");
+  }
+  rg::stage_wait_probe_kernel<<<1, 64, 0, static_cast<cudaStream_t>(stream)>>>(pl->d_status, polls);
+  RG_CUDA_TRY(cudaGetLastError());
   return RG_OK;
 }
 

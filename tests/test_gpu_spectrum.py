@@ -219,6 +219,28 @@ def test_batched_rejects_bad_offsets(gpu, oracle_lib):
     assert torch.isfinite(out).all()
 
 
+def test_stage_wait_timeout_is_reported_and_recoverable(gpu, oracle_lib):
+    """A bounded wait that gives up (a barrier phase nothing completes) surfaces as
+    RG_ERR_TIMEOUT at the next check; the record clears and the context keeps working."""
+    P = particles(2000, seed=4)
+    T, prt = to_device(P, gpu)
+    plan = capi.SpectrumPlan(oracle_lib.logspace(0.01, 1e7, 64), 1.0, 1.0, 1.0)
+    ref = torch.empty(64, device=gpu)
+    plan.run(prt, ref)
+    plan.check()
+    with pytest.raises(capi.RgError, match="out of range|polls"):
+        plan.probe_stage_timeout(0)
+    plan.probe_stage_timeout(256)
+    with pytest.raises(capi.RgError, match="bounded wait") as e:
+        plan.check()
+    assert e.value.status == capi.RG_ERR_TIMEOUT
+    plan.check()  # cleared
+    out = torch.empty(64, device=gpu)
+    plan.run(prt, out)
+    plan.check()
+    assert torch.equal(out, ref)
+
+
 def test_full_size_properties(gpu):
     """Config-2 scale (1e8 particles, 512 bins): additivity over a batched split,
     exact scaling by powers of two, bit-identical reruns."""
