@@ -91,6 +91,35 @@ def test_edge_energies(gpu, oracle_lib, log_spaced, fourvel):
     check_against_oracle(oracle_lib, ux, z, z, bins, log_spaced, fourvel, gpu)
 
 
+@pytest.mark.parametrize("kind", ["log4096", "lin4096", "narrow", "float_overflow"])
+@pytest.mark.parametrize("fourvel", [True, False])
+def test_bin_lookup_cell_table(gpu, oracle_lib, kind, fourvel):
+    """Bin sets whose float-bit cell table holds several thresholds per cell (4096 bins),
+    spans a tiny range (1 .. 1.0001), or has no finite threshold at all (bins 1e-30 .. 1e30:
+    the reference's float emax / emin overflows, so every finite energy lands in bin 0):
+    counts bit-exact against the oracle for random particles and for |u| within 2 ulp of the
+    square root of every finite threshold."""
+    log_spaced = kind in ("log4096", "float_overflow")
+    bins = {"log4096": lambda: oracle_lib.logspace(1e-4, 1e9, 4096),
+            "lin4096": lambda: oracle_lib.linspace(0.01, 1e3, 4096),
+            "narrow": lambda: oracle_lib.linspace(1.0, 1.0001, 50),
+            "float_overflow": lambda: oracle_lib.logspace(1e-30, 1e30, 300)}[kind]()
+    nb = len(bins)
+    thr = np.empty(nb, np.float32)
+    nan_idx = ctypes.c_int32()
+    capi.check(capi.lib().rg_energy_thresholds(bins.ctypes.data, nb, int(fourvel), thr.ctypes.data,
+                                               ctypes.byref(nan_idx)))
+    # |u| within 2 ulp of sqrt(threshold): Usqr = |u|^2 lands on both sides of every threshold
+    s = np.sqrt(thr[1:][np.isfinite(thr[1:])].astype(np.float64)).astype(np.float32)
+    lo1, hi1 = np.nextafter(s, np.float32(0)), np.nextafter(s, np.float32(np.inf))
+    edge = np.concatenate([s, lo1, hi1, np.nextafter(lo1, np.float32(0)), np.nextafter(hi1, np.float32(np.inf)),
+                           np.array([0.0, 1e-23, 1e-15, 1.0, 1.7e19, np.inf], np.float32)]).astype(np.float32)
+    P = particles(100_000, seed=17)
+    z = np.zeros_like(edge)
+    ux, uy, uz = (np.concatenate([a, P[k]]) for a, k in ((edge, "ux"), (z, "uy"), (z, "uz")))
+    check_against_oracle(oracle_lib, ux, uy, uz, bins, log_spaced, fourvel, gpu)
+
+
 def test_nan_and_inf_inputs(gpu, oracle_lib):
     ux = np.array([np.nan, np.inf, -np.inf, 3.0, 0.0], np.float32)
     z = np.zeros_like(ux)
