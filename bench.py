@@ -522,6 +522,7 @@ def run_ours(args, rank, world, local_rank):
         extra["fromdist_gemm_4096x1024x1024"]["peak_source"] = peak_src
         extra["adam_fit_1024x512x512"] = guarded(adam_fit_case, torch, capi, device)
         extra["ic_1024x1024x1024"] = guarded(ic_case, torch, capi, device, clocks.get("sm_mhz") or 2070.0)
+        add_wavefront_rooflines(extra, sms, clocks.get("sm_mhz") or 2070.0)
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     result["extra"] = extra
@@ -529,6 +530,33 @@ def run_ours(args, rank, world, local_rank):
     plan_p.close()
     if rank == 0:
         print(json.dumps(result), flush=True)
+
+
+def wavefront_roofline(achieved, evals_per_sm_clock, sms, clk_mhz, basis):
+    """Fraction of the rate the shared-memory table reads allow (one wavefront per SM-clock)."""
+    peak = sms * clk_mhz * 1e6 * evals_per_sm_clock
+    return {"bound": "shared-memory wavefronts", "achieved": achieved, "peak": peak, "unit": "evals/s",
+            "frac": achieved / peak, "basis": basis}
+
+
+def add_wavefront_rooflines(extra, sms, clk_mhz):
+    """Roofline fractions of the batched forward and of the forward + adjoint pair."""
+    bg = extra.get("batched_graph_256_segments", {})
+    if "graph_evals_per_s" in bg:
+        bg["roofline"] = wavefront_roofline(
+            bg["graph_evals_per_s"], 8.0, sms, clk_mhz,
+            "200 bins 0.045 dex apart over 0.040-dex table segments: each 32-lane 8-byte lookup takes 4 "
+            "wavefronts (16 lanes touch ~18 distinct entries), so 8 evals per SM-clock")
+    fa = extra.get("fwd_adjoint_1e7x512", {})
+    if "fwd_plus_adjoint_evals_per_s" in fa:
+        basis = ("smooth table: every lane reads its own 16-byte Hermite segment, at least 4 wavefronts "
+                 "per 32 evals in each kernel")
+        fa["roofline"] = wavefront_roofline(fa["fwd_plus_adjoint_evals_per_s"], 4.0, sms, clk_mhz,
+                                            basis + "; forward + adjoint = two passes, 4 evals per SM-clock")
+        fa["roofline_fwd"] = wavefront_roofline(fa["fwd_evals_per_s"], 8.0, sms, clk_mhz,
+                                                basis + ": 8 evals per SM-clock")
+        fa["roofline_adjoint"] = wavefront_roofline(fa["adjoint_evals_per_s"], 8.0, sms, clk_mhz,
+                                                    basis + ": 8 evals per SM-clock")
 
 
 def guarded(fn, *a):
