@@ -143,6 +143,14 @@ def photon_bins():
     return bins
 
 
+def photon_bins_cpu():
+    """The same 512 photon bins for the CPU legs, from the oracle's Logspace (bit-identical
+    to the library's): a CPU-only process must not load the product library."""
+    import oracle  # noqa: PLC0415
+
+    return oracle.logspace(BIN_LO, BIN_HI, NBINS)
+
+
 # ---------------------------------------------------------------------------------------
 # clocks
 # ---------------------------------------------------------------------------------------
@@ -237,7 +245,7 @@ def cpu_spectrum_runner():
 
 def cpu_baseline(target_seconds: float):
     kind, fn, threads = cpu_spectrum_runner()
-    bins = photon_bins()
+    bins = photon_bins_cpu()
     # calibrate on a small sample, then time one bounded sample of ~target_seconds
     calib = make_particles_numpy(20000, seed=7)
     t0 = time.perf_counter()
@@ -256,7 +264,7 @@ def run_reference_arm(args, rank):
     if rank != 0:
         return
     kind, fn, threads = cpu_spectrum_runner()
-    bins = photon_bins()
+    bins = photon_bins_cpu()
     calib = make_particles_numpy(20000, seed=7)
     t0 = time.perf_counter()
     fn(calib, bins)
@@ -383,6 +391,9 @@ def run_ours(args, rank, world, local_rank):
     spectra_ok = bool(torch.isfinite(out_e).all() and torch.isfinite(out_p).all() and out_e.sum() > 0)
     if dist:
         t_step = shard.max_over_ranks(t_step, device)
+    device_spectra = torch.cat([out_e, out_p[None]]).cpu().numpy()
+    parity = guarded(headline_parity, torch, capi, comps, n_per, bins, plan_e, plan_p, stream) \
+        if rank == 0 else None
 
     # fused-kernel roofline: FP32-core issue slots (SMs x 128 lanes x clock)
     kern_ms = (ke_ms + kp_ms) / max(ke_n + kp_n, 1)
@@ -417,6 +428,8 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
     }
 
+    if parity is not None:
+        result["parity_vs_fp64"] = parity
     extra = {"spectra_finite": spectra_ok}
     if rank == 0 and not args.no_extras:
         extra["energy_distribution_dump"] = guarded(histogram_case, torch, capi, device, comps, NSPECIES * n_per)
@@ -426,8 +439,11 @@ def run_ours(args, rank, world, local_rank):
         host = [torch.empty(c.numel(), dtype=torch.float32, pin_memory=True) for c in comps]
         for h, c in zip(host, comps):
             h.copy_(c)
+        breakdown = {"kernel_only": guarded(kernel_only_steps, torch, capi, comps, n_per,
+                                            [plan_e, plan_e, plan_p], stream, max(args.steps, 1))}
         del comps, u, b, w
         torch.cuda.empty_cache()
+        breakdown["copy_only"] = guarded(copy_only_steps, torch, host, n_per, device, max(args.steps, 1))
         depth = 3  # steps in flight when pipelined
         houts = [torch.empty((3, NBINS), dtype=torch.float32, pin_memory=True) for _ in range(depth)]
         douts = [torch.empty((3, NBINS), device=device) for _ in range(depth)]
@@ -493,7 +509,16 @@ def run_ours(args, rank, world, local_rank):
 
         t_e2e, ok_p = timed_e2e(run_pipelined)
         t_sync, ok_s = timed_e2e(run_synchronous)
-        t_med = statistics.median(step_times(max(args.steps, 1)))
+        e2e_steps = step_times(max(args.steps, 1))
+        t_med = statistics.median(e2e_steps)
+        breakdown["e2e_step_synchronous"] = step_stats(e2e_steps)
+        # the host path's spectra against the device-resident ones of the same particles
+        # (the chunks sum in another order, so they agree to FP32 rounding, not bit for bit)
+        e2e_spectra = houts[(max(args.steps, 1) - 1) % depth].numpy().astype("float64")
+        ref_spectra = device_spectra.astype("float64")
+        nz = ref_spectra > 1e-12 * ref_spectra.max(axis=1, keepdims=True)
+        breakdown["e2e_vs_device_max_rel_diff"] = float(
+            (abs(e2e_spectra - ref_spectra)[nz] / ref_spectra[nz]).max())
         spectra_ok = spectra_ok and ok_p and ok_s
         extra["spectra_finite"] = spectra_ok
         result["e2e"] = {"value": world * evals_per_step / t_e2e, "unit": UNIT,
@@ -502,6 +527,7 @@ def run_ours(args, rank, world, local_rank):
                          "ms_per_step": t_e2e * 1e3,
                          "value_step_synchronous": world * evals_per_step / t_sync,
                          "ms_per_step_synchronous_median": t_med * 1e3,
+                         "breakdown": breakdown,
                          "path": "rg_spectrum_run_host per species (pinned host SoA, chunked H2D through the "
                                  "device's staging pipeline, overlapped with the fused kernel) + D2H of the "
                                  "3 spectra every step; steps pipelined (up to 3 steps enqueued before the "
@@ -530,6 +556,116 @@ def run_ours(args, rank, world, local_rank):
     plan_p.close()
     if rank == 0:
         print(json.dumps(result), flush=True)
+
+
+def step_stats(ts):
+    """Mean, median and 95th percentile of per-step wall times, in ms."""
+    s = sorted(ts)
+    return {"steps": len(s), "mean_ms": 1e3 * sum(s) / len(s), "median_ms": 1e3 * statistics.median(s),
+            "p95_ms": 1e3 * s[min(len(s) - 1, int(math.ceil(0.95 * len(s))) - 1)]}
+
+
+def kernel_only_steps(torch, capi, comps, n_per, plans, stream, k):
+    """The e2e step without its input copies: the three species' spectra from
+    device-resident particles (one rg_spectrum_run each) and the D2H read of the three
+    spectra, each step waited for (host wall clock per step)."""
+    device = comps[0].device
+    species = []
+    for s in range(NSPECIES):
+        sl = slice(s * n_per, (s + 1) * n_per)
+        species.append(capi.particles([c[sl] for c in comps[0:3]], b=[c[sl] for c in comps[3:6]],
+                                      w=comps[6][sl], n=n_per))
+    d = torch.empty((NSPECIES, NBINS), device=device)
+    h = torch.empty((NSPECIES, NBINS), dtype=torch.float32, pin_memory=True)
+
+    def one():
+        for s in range(NSPECIES):
+            plans[s].run(species[s], d[s], stream)
+        h.copy_(d, non_blocking=True)
+        torch.cuda.current_stream(device).synchronize()
+
+    for _ in range(3):
+        one()
+    ts = []
+    for _ in range(k):
+        t0 = time.perf_counter()
+        one()
+        ts.append(time.perf_counter() - t0)
+    return step_stats(ts)
+
+
+def copy_only_steps(torch, host, n_per, device, k, chunk=1 << 22):
+    """The e2e step's input copies without its kernels: the same 7 components x 3 species
+    in the same 2^22-particle chunks, pinned host -> two alternating device staging
+    buffers on one copy stream (as the library's host staging issues them), each step
+    waited for (host wall clock per step)."""
+    stage = [torch.empty((len(host), chunk), device=device) for _ in range(2)]
+    cs = torch.cuda.Stream(device)
+
+    def one():
+        i = 0
+        with torch.cuda.stream(cs):
+            for s in range(NSPECIES):
+                for a in range(0, n_per, chunk):
+                    m = min(chunk, n_per - a)
+                    buf = stage[i % 2]
+                    for c, hc in enumerate(host):
+                        buf[c, :m].copy_(hc[s * n_per + a:s * n_per + a + m], non_blocking=True)
+                    i += 1
+        cs.synchronize()
+
+    for _ in range(3):
+        one()
+    ts = []
+    for _ in range(k):
+        t0 = time.perf_counter()
+        one()
+        ts.append(time.perf_counter() - t0)
+    out = step_stats(ts)
+    out["bytes_per_step"] = 4 * len(host) * NSPECIES * n_per
+    out["gbs_median"] = out["bytes_per_step"] / (out["median_ms"] * 1e-3) / 1e9
+    return out
+
+
+def headline_parity(torch, capi, comps, n_per, bins, plan_e, plan_p, stream, m=1_000_000):
+    """Per-bin error of the headline spectra against the FP64 oracle, per species: the
+    last m e- particles and the first m e+ particles as two segments of the e+- plan's
+    batched launch, the first m protons through the proton plan (e_syn_at_g_syn / 1836),
+    weights included; the oracle (FP64 restatement of synchrotron.cpp:107-145) runs on the
+    same particles.  Error = max over bins above 1e-12 of the peak of |S - S64| / S64."""
+    import numpy as np  # noqa: PLC0415
+
+    import oracle  # noqa: PLC0415
+
+    device = comps[0].device
+    offs = torch.tensor([n_per - m, n_per, n_per + m], dtype=torch.int64, device=device)
+    prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=NSPECIES * n_per)
+    got_e = torch.empty((2, NBINS), device=device)
+    plan_e.run_batched(prt, offs, 2, got_e, stream)
+    p0 = 2 * n_per
+    sl = slice(p0, p0 + m)
+    prt_p = capi.particles([c[sl] for c in comps[0:3]], b=[c[sl] for c in comps[3:6]], w=comps[6][sl], n=m)
+    got_p = torch.empty(NBINS, device=device)
+    plan_p.run(prt_p, got_p, stream)
+    torch.cuda.synchronize()
+    plan_e.check(stream)
+    plan_p.check(stream)
+    table = oracle.tabulate_ffunc()
+    keys = ("ux", "uy", "uz", "bx", "by", "bz", "w")
+    res = {"particles_per_species": m, "bins_compared": "bins above 1e-12 of the species' peak",
+           "oracle": "FP64 restatement of the reference path (float table and bins as data)"}
+    t0 = time.perf_counter()
+    for name, a, eps, got in (("e-", n_per - m, 1.0, got_e[0]), ("e+", n_per, 1.0, got_e[1]),
+                              ("p", p0, 1.0 / PROTON_MASS_RATIO, got_p)):
+        P = {k: comps[i][a:a + m].cpu().numpy() for i, k in enumerate(keys)}
+        ref = oracle.sync_spectrum_f64(P, bins, 1.0, 1.0, eps, table)
+        g = got.cpu().numpy().astype(np.float64)
+        mask = ref > 1e-12 * ref.max()
+        res[name] = {"max_rel_err_vs_fp64": float(np.max(np.abs(g[mask] - ref[mask]) / ref[mask])),
+                     "bins_compared": int(mask.sum())}
+    res["oracle_seconds"] = time.perf_counter() - t0
+    res["max_rel_err_vs_fp64"] = max(res[s]["max_rel_err_vs_fp64"] for s in ("e-", "e+", "p"))
+    return res
 
 
 def wavefront_roofline(achieved, evals_per_sm_clock, sms, clk_mhz, basis):

@@ -42,12 +42,20 @@ enum {
   RG_TABLE_SMOOTH    = 1  /* exact F on a fine log grid, C1 cubic Hermite (differentiable) */
 };
 
+/* How a reference-table particle plan sums its spectrum (rg_spectrum_plan_set_algorithm). */
+enum {
+  RG_ALGO_AUTO    = 0, /* interval moments where the plan supports them, else the fused kernel */
+  RG_ALGO_DIRECT  = 1, /* the fused kernel: every (particle, bin) pair evaluated in FP32 */
+  RG_ALGO_MOMENTS = 2  /* interval moments: exact FP64 sums per (table cell, bin interval) */
+};
+
 /* --------------------------------------------------------------------------
  * Runtime
  * ------------------------------------------------------------------------ */
 
-/* rg.Initialize (pyinterface.cpp:30-38): select `device`, create the context and
- * build the default F table.  Idempotent. */
+/* rg.Initialize (pyinterface.cpp:30-38): select `device`, create the context,
+ * build the default F table and make rg_synchrotron_spectrum_noalloc's fixed
+ * device array and kernels resident.  Idempotent. */
 int rg_init(int device);
 
 /* rg.Finalize (pyinterface.cpp:40-49): release cached plans and tables. */
@@ -176,6 +184,20 @@ int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p,
 int rg_spectrum_run_host(rg_spectrum_plan* plan, const rg_particles* p, float* out,
                          void* stream);
 
+/* Chooses how a reference-table particle plan sums its spectrum: RG_ALGO_AUTO
+ * (the default: interval moments when the plan supports them, the fused kernel
+ * otherwise), RG_ALGO_DIRECT (the fused kernel, which evaluates every (particle,
+ * bin) pair in FP32 and is bit-reproducible) or RG_ALGO_MOMENTS (fails with
+ * RG_ERR_UNSUPPORTED at run time where the plan cannot take it: smooth table,
+ * distribution source, more than 1024 segments).  Both compute the reference's
+ * sum over particles and bins of synchrotron.hpp:145-172; interval moments sum
+ * the piecewise-linear F exactly in FP64 per (table cell, bin interval), with
+ * FP64 atomics (independent of particle order to FP64 rounding).  No reference
+ * counterpart. */
+int rg_spectrum_plan_set_algorithm(rg_spectrum_plan* plan, int32_t algo);
+/* The algorithm a run over `nseg` segments would use (RG_ALGO_DIRECT or RG_ALGO_MOMENTS). */
+int rg_spectrum_plan_algorithm(const rg_spectrum_plan* plan, int32_t nseg, int32_t* algo);
+
 /* Kernel timing: when enabled, every fused-kernel launch of `plan` is bracketed
  * by CUDA events on its stream.  rg_spectrum_plan_kernel_time synchronises those
  * events and returns the summed kernel time (ms) and the launch count since the
@@ -202,11 +224,15 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
  * comes from one fixed file-scope device array of about 1.4 MB that each GPU
  * loading the library keeps until exit, and the call makes no cudaMalloc,
  * cudaFree or other allocating call.  At most 512 photon bins (larger counts are
- * rejected with RG_ERR_ARGUMENT).  The first call on a device looks up the
- * array's address and builds the F table into it, synchronising the device's
- * default stream: make it before any stream capture.  All calls share the
- * array: calls whose GPU work overlaps race on it.  A device-side failure shows
- * as NaN outputs. */
+ * rejected with RG_ERR_ARGUMENT; nbins = 0 does nothing).  The array and the
+ * kernels exist on a device once their code is loaded there (CUDA loads modules
+ * lazily, on first use): rg_init(device) loads them, looks up the array's
+ * address and builds the F table into it, so call rg_init on every device
+ * before handing its memory out.  Without it, the first call on a device does
+ * that set-up itself, needs device memory for it at that moment and
+ * synchronises the device's default stream: it must then come before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps
+ * race on it.  A device-side failure shows as NaN outputs. */
 int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, int32_t nbins, float B0,
                                     float g_syn, float e_syn_at_g_syn, float* out, void* stream);
 

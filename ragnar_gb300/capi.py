@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libragnar_gb300.so")
 HEADER = os.path.join(os.path.dirname(_HERE), "include", "ragnar_gb300.h")
 
 RG_OK = 0
+RG_ALGO_AUTO, RG_ALGO_DIRECT, RG_ALGO_MOMENTS = 0, 1, 2
 RG_ERR_ARGUMENT = 1
 RG_ERR_CUDA = 2
 RG_ERR_TIMEOUT = 3
@@ -85,6 +86,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_run_plain": [_vp, ctypes.POINTER(Particles), _vp, _vp],
         "rg_spectrum_run_host": [_vp, ctypes.POINTER(Particles), _vp, _vp],
         "rg_spectrum_plan_enable_timing": [_vp, _i32],
+        "rg_spectrum_plan_set_algorithm": [_vp, _i32],
+        "rg_spectrum_plan_algorithm": [_vp, _i32, ctypes.POINTER(_i32)],
         "rg_spectrum_plan_kernel_time": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64)],
         "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
         "rg_synchrotron_spectrum_noalloc": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp,
@@ -210,6 +213,16 @@ class SpectrumPlan:
 
     def enable_timing(self, on: bool = True) -> None:
         check(lib().rg_spectrum_plan_enable_timing(self.handle, int(on)))
+
+    def set_algorithm(self, algo: int) -> None:
+        """RG_ALGO_AUTO, RG_ALGO_DIRECT (the fused per-eval kernel) or RG_ALGO_MOMENTS."""
+        check(lib().rg_spectrum_plan_set_algorithm(self.handle, algo))
+
+    def algorithm(self, nseg: int = 1) -> int:
+        """The algorithm a run over nseg segments would use."""
+        a = _i32()
+        check(lib().rg_spectrum_plan_algorithm(self.handle, nseg, ctypes.byref(a)))
+        return a.value
 
     def kernel_time(self) -> tuple[float, int]:
         """(summed fused-kernel milliseconds, launches) since the last call."""

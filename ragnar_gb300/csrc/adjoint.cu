@@ -383,6 +383,7 @@ extern "C" {
 
 int rg_spectrum_adjoint(const rg_spectrum_plan* cplan, const rg_particles* p, const float* grad_out,
                         float* grad_w, float* grad_ux, float* grad_uy, float* grad_uz, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumAdjoint");
   auto* plan = const_cast<rg_spectrum_plan*>(cplan);
   if (!plan || !grad_out || plan->source != rg::kSrcParticles) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_adjoint: bad arguments");
@@ -398,6 +399,7 @@ int rg_spectrum_adjoint(const rg_spectrum_plan* cplan, const rg_particles* p, co
 int rg_spectrum_adjoint_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
                                 int32_t nseg, const float* grad_out, float* grad_w, float* grad_ux,
                                 float* grad_uy, float* grad_uz, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumAdjoint");
   if (!plan || !offsets || nseg < 0 || !grad_out || plan->source != rg::kSrcParticles) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_adjoint_batched: bad arguments");
   }
@@ -421,6 +423,7 @@ int rg_dist_plan_create(const float* bins, int32_t nbins, float g_syn, float e_s
 
 int rg_dist_adjoint(const rg_spectrum_plan* plan, const float* gbeta, const float* f, int32_t ng,
                     const float* grad_out, float* grad_f, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumFromDistAdjoint");
   if (!plan || plan->source != rg::kSrcDist || ng < 0 || !grad_out || (ng > 0 && (!gbeta || !f))) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_dist_adjoint: bad arguments");
   }

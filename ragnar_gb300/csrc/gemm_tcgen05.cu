@@ -1027,6 +1027,7 @@ int rg_fromdist_plan_destroy(rg_fromdist_plan* pl) {
 }
 
 int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumFromDist");
   if (!pl || ndist < 0 || ndist > pl->max_dist || (ndist > 0 && (!f || !out))) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_run: bad arguments (ndist above the plan's max_dist?)");
   }
@@ -1052,6 +1053,7 @@ int rg_fromdist_run(rg_fromdist_plan* pl, const float* f, int32_t ndist, float* 
 }
 
 int rg_fromdist_adjoint(rg_fromdist_plan* pl, const float* grad_out, int32_t ndist, float* grad_f, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumFromDistAdjoint");
   if (!pl || ndist < 0 || ndist > pl->max_dist || (ndist > 0 && (!grad_out || !grad_f))) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_fromdist_adjoint: bad arguments (ndist above the plan's max_dist?)");
   }

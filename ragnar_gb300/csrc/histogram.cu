@@ -468,6 +468,7 @@ int rg_energy_thresholds(const float* bins, int32_t nbins, int32_t fourvel, floa
 int rg_energy_distribution(const float* ux, const float* uy, const float* uz, int64_t n,
                            const float* bins, int32_t nbins, int32_t log_spaced, int32_t fourvel,
                            float* hist, uint64_t* counts, void* stream) {
+  rg::NvtxRange nvtx_range("ComputeEnergyDistribution");
   rg::clear_error();
   if (nbins < 1 || !bins || !hist || n < 0 || (n > 0 && (!ux || !uy || !uz))) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_energy_distribution: bad arguments");

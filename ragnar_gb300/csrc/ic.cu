@@ -228,6 +228,7 @@ extern "C" {
 
 int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_spaced, const float* es,
                    const float* fs, int32_t ns, const float* eic, int32_t ne, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("ICSpectrum");
   rg::clear_error();
   if (ng < 0 || ns < 0 || ne < 0 || (ng > 0 && (!gbins || !f)) || (ns > 0 && (!es || !fs)) ||
       (ne > 0 && (!eic || !out))) {

@@ -14,10 +14,15 @@
 //  * at most kNoAllocMaxBins (512) photon bins, reference table only; the
 //    array is kNoAllocBytes (about 1.4 MB) and every GPU that loads the
 //    library holds it until the process exits;
-//  * the first call on a device (with that device current) looks up the
-//    array's device address with cudaGetSymbolAddress and builds the F table
-//    into it, synchronising the device's default stream; make that first call
-//    before any stream capture;
+//  * the array and the kernels this entry point launches come into existence
+//    on a device when their code is loaded there, which CUDA's lazy module
+//    loading does on first use; rg_init(device) does it up front: it looks up
+//    the array's device address with cudaGetSymbolAddress, loads the kernels and
+//    builds the F table into the array (synchronising the device's default
+//    stream).  Call rg_init for every device before handing the device memory
+//    budget out; without it, the first call on a device does this set-up
+//    itself, needs device memory for the code and the array at that moment, and
+//    should come before any stream capture;
 //  * every call shares the array and it keeps the last call's contents; each
 //    call rewrites what it reads and clears the status word itself, but calls
 //    whose GPU work overlaps (on different streams or threads) race on it;
@@ -35,6 +40,7 @@
 namespace rg {
 
   int launch_fused_reference(int K, const FusedParams& fp, int grid, cudaStream_t s);
+  int preload_reference_kernels();
   int launch_reduce_single(const double* partials, int grid, int64_t n, int nbins, const float* ebins,
                            const uint8_t* valid, const unsigned* status, float* out, cudaStream_t s);
   int build_reference_table_into(int n, float xmin, float xmax, float* d_x, float* d_y, float2* d_coef,
@@ -83,12 +89,14 @@ namespace rg {
       return m;
     }
 
-    // Once per device, with that device current.
+    // Once per device, with that device current: the array's device address (looking
+    // it up loads this file's module, which holds the array), the kernels, the F table.
     int noalloc_setup(int dev, NoAllocDevice& d) {
       void* ptr = nullptr;
       RG_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
       d.base = static_cast<unsigned char*>(ptr);
       RG_CUDA_TRY(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+      RG_TRY(preload_reference_kernels());
       RG_TRY(build_reference_table_into(kTableNodes, 1e-6f, 100.0f, reinterpret_cast<float*>(d.base + kOffTabX),
                                         reinterpret_cast<float*>(d.base + kOffTabY),
                                         reinterpret_cast<float2*>(d.base + kOffCoef),
@@ -96,7 +104,27 @@ namespace rg {
       return RG_OK;
     }
 
+    // The device's set-up record, made on first use (under the mutex).
+    int noalloc_device(int dev, NoAllocDevice& out) {
+      std::lock_guard<std::mutex> lock(noalloc_mutex());
+      auto                        it = noalloc_devices().find(dev);
+      if (it == noalloc_devices().end()) {
+        NoAllocDevice fresh;
+        RG_TRY(noalloc_setup(dev, fresh));
+        it = noalloc_devices().emplace(dev, fresh).first;
+      }
+      out = it->second;
+      return RG_OK;
+    }
+
   } // namespace
+
+  // Called by rg_init with `dev` current, so that the array and the kernels are resident
+  // before a caller hands its device memory out.
+  int noalloc_prepare(int dev) {
+    NoAllocDevice d;
+    return noalloc_device(dev, d);
+  }
 
 } // namespace rg
 
@@ -104,33 +132,31 @@ extern "C" {
 
 int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, int32_t nbins, float B0,
                                     float g_syn, float e_syn_at_g_syn, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
   using namespace rg;
   clear_error();
   if (!p || p->n < 0 || (p->n > 0 && (!p->u[0] || !p->u[1] || !p->u[2]))) {
     return set_error(RG_ERR_ARGUMENT, "particles need U1..U3 device arrays and n >= 0");
   }
-  if (nbins < 1 || nbins > kNoAllocMaxBins || !bins || !out) {
-    return set_error(RG_ERR_ARGUMENT, "rg_synchrotron_spectrum_noalloc: needs 1 to " +
+  if (nbins < 0 || nbins > kNoAllocMaxBins || (nbins > 0 && (!bins || !out))) {
+    return set_error(RG_ERR_ARGUMENT, "rg_synchrotron_spectrum_noalloc: needs 0 to " +
                                         std::to_string(kNoAllocMaxBins) + " photon bins (got " +
                                         std::to_string(nbins) + ") and an output array");
   }
   if (B0 == 0.0f) {
     return set_error(RG_ERR_ARGUMENT, "B0 must be non-zero");
   }
+  if (nbins == 0) { // as rg_synchrotron_spectrum: nothing to compute
+    return RG_OK;
+  }
   int dev = 0;
   RG_CUDA_TRY(cudaGetDevice(&dev));
   NoAllocDevice d;
-  {
-    std::lock_guard<std::mutex> lock(noalloc_mutex());
-    auto                        it = noalloc_devices().find(dev);
-    if (it == noalloc_devices().end()) {
-      NoAllocDevice fresh;
-      RG_TRY(noalloc_setup(dev, fresh));
-      it = noalloc_devices().emplace(dev, fresh).first;
-    }
-    d = it->second;
-  }
+  RG_TRY(noalloc_device(dev, d));
   auto s = static_cast<cudaStream_t>(stream);
+  // the caller may change or free `bins` once this returns, even if it is pinned
+  // memory (whose copy would otherwise still be in flight): copy from a host vector
+  const std::vector<float> hB(bins, bins + nbins);
 
   // e_peak = K0 gamma sqrt(W), K0 = eps / (g^2 B0): K0 <= 0 means no emission
   const double K0 = static_cast<double>(e_syn_at_g_syn) /
@@ -149,7 +175,7 @@ int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, in
   std::vector<uint8_t> hV(kNoAllocMaxBins, 0);
   int64_t              pmin = std::numeric_limits<int64_t>::max(), pmax = std::numeric_limits<int64_t>::min();
   for (int j = 0; j < nbins; ++j) {
-    const double e = bins[j];
+    const double e = hB[j];
     if (!(e > 0.0) || !std::isfinite(e)) {
       continue;
     }
@@ -178,7 +204,7 @@ int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, in
   RG_CUDA_TRY(cudaMemsetAsync(b + kOffStatus, 0, sizeof(unsigned), s));
   RG_CUDA_TRY(cudaMemcpyAsync(b + kOffP, hP.data(), sizeof(int32_t) * kSliceBins, cudaMemcpyHostToDevice, s));
   RG_CUDA_TRY(cudaMemcpyAsync(b + kOffRange, hR, sizeof(hR), cudaMemcpyHostToDevice, s));
-  RG_CUDA_TRY(cudaMemcpyAsync(b + kOffEbins, bins, sizeof(float) * nbins, cudaMemcpyHostToDevice, s));
+  RG_CUDA_TRY(cudaMemcpyAsync(b + kOffEbins, hB.data(), sizeof(float) * nbins, cudaMemcpyHostToDevice, s));
   RG_CUDA_TRY(cudaMemcpyAsync(b + kOffValid, hV.data(), nbins, cudaMemcpyHostToDevice, s));
 
   FusedParams fp {};

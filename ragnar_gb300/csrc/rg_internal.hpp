@@ -4,6 +4,7 @@
 #include "ragnar_gb300.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
@@ -54,6 +55,18 @@ namespace rg {
     }
     return e;
   }
+
+  // NVTX range around one C-ABI call, named after the Kokkos label the reference gives the
+  // same work (synchrotron.cpp:92,131 "SynchrotronSpectrum", particles.cpp:225
+  // "ComputeEnergyDistribution", ic.cpp:38 "ICSpectrum"), so a profiler shows the stages
+  // under the reference's names.  NVTX v3 is header-only: without an attached tool each
+  // push and pop is a test of a null function pointer.
+  struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&)            = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+  };
 
   // Scratch device buffer freed when it leaves scope (also on an early error return).
   template <typename T>
@@ -138,6 +151,9 @@ namespace rg {
   // Builds the reference table on `n` nodes of Logspace(xmin, xmax) (FP64 on the GPU).
   int build_reference_table(int n, float xmin, float xmax, RefTable& t, cudaStream_t s);
   int build_smooth_table(SmoothTable& t, cudaStream_t s);
+  // Makes the allocation-free entry point's scratch array and kernels resident on `dev`
+  // (the current device) and builds its F table; noalloc.cu.
+  int noalloc_prepare(int dev);
   void free_tables(DeviceContext& c);
   void free_staging(DeviceContext& c);
   // Device copies of the histogram's bin thresholds (histogram.cu).

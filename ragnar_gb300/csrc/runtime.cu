@@ -163,7 +163,9 @@ int rg_init(int device) {
   RG_CUDA_TRY(cudaSetDevice(device));
   RG_CUDA_TRY(cudaFree(nullptr)); // create the primary context
   const rg::RefTable* t = nullptr;
-  return rg::reference_table(&t);
+  RG_TRY(rg::reference_table(&t));
+  // the allocation-free entry point's array and kernels, made resident now
+  return rg::noalloc_prepare(device);
 }
 
 int rg_finalize(void) {

@@ -531,11 +531,17 @@ namespace rg {
       return tab + sizeof(int2) * 2 * kChunk + sizeof(float) * 2 * nslots * kChunkPad;
     }
 
+    // Sets the kernel's shared-memory limit once per device (which also loads it).
+    template <int K, int MODE>
+    cudaError_t configure_fused_k() {
+      static std::atomic<uint64_t> configured { 0 };
+      return ensure_max_dynamic_smem(fused_spectrum_kernel<K, MODE>,
+                                     static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)), configured);
+    }
+
     template <int K, int MODE>
     cudaError_t launch_fused_k(const FusedParams& fp, dim3 grid, size_t smem, cudaStream_t s) {
-      static std::atomic<uint64_t> configured { 0 };
-      const cudaError_t            e = ensure_max_dynamic_smem(
-        fused_spectrum_kernel<K, MODE>, static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)), configured);
+      const cudaError_t e = configure_fused_k<K, MODE>();
       if (e != cudaSuccess) {
         return e;
       }
@@ -668,7 +674,7 @@ namespace rg {
         RG_CUDA_TRY(cudaMemcpy(pl->d_ebins, pl->h_bins.data(), sizeof(float) * pl->nbins,
                                cudaMemcpyHostToDevice));
       }
-      return RG_OK;
+      return moments_prepare(pl, hV, ln_xmin, dln, ln_k0);
     }
 
     int create_plan_common(rg_spectrum_plan* pl, const float* bins, int32_t nbins) {
@@ -725,6 +731,17 @@ namespace rg {
       pl->d_prefix = nullptr;
       RG_CUDA_TRY(cudaMalloc(&pl->d_prefix, sizeof(int64_t) * (max_seg + 1)));
       pl->prefix_cap = max_seg;
+    }
+    // the interval moments of max_seg segments, so that runs allocate nothing (and can be
+    // captured in a CUDA graph)
+    if (moments_selected(pl, max_seg)) {
+      const size_t need = static_cast<size_t>(max_seg) * static_cast<size_t>(pl->hist_per_seg);
+      if (need > pl->hist_cap) {
+        cudaFree(pl->d_hist);
+        pl->d_hist = nullptr;
+        RG_CUDA_TRY(cudaMalloc(&pl->d_hist, sizeof(double2) * need));
+        pl->hist_cap = need;
+      }
     }
     return RG_OK;
   }
@@ -793,6 +810,20 @@ namespace rg {
     return RG_OK;
   }
 
+  // Loads the reference-table fused kernels (every row count K) and the reduction on the
+  // current device, so that a later launch needs no module load (a load reserves device
+  // memory for the code under CUDA's lazy loading).
+  int preload_reference_kernels() {
+#define RG_K_LOAD(k) RG_CUDA_TRY((configure_fused_k<k, kModeRef>()));
+    RG_K_LOAD(1) RG_K_LOAD(2) RG_K_LOAD(3) RG_K_LOAD(4) RG_K_LOAD(5) RG_K_LOAD(6) RG_K_LOAD(7) RG_K_LOAD(8)
+    RG_K_LOAD(9) RG_K_LOAD(10) RG_K_LOAD(11) RG_K_LOAD(12) RG_K_LOAD(13) RG_K_LOAD(14) RG_K_LOAD(15)
+    RG_K_LOAD(16)
+#undef RG_K_LOAD
+    cudaFuncAttributes attr {};
+    RG_CUDA_TRY(cudaFuncGetAttributes(&attr, reduce_partials_kernel));
+    return RG_OK;
+  }
+
   int launch_reduce_single(const double* partials, int grid, int64_t n, int nbins, const float* ebins,
                            const uint8_t* valid, const unsigned* status, float* out, cudaStream_t s) {
     ReduceParams rp {};
@@ -858,6 +889,14 @@ namespace rg {
       if (pl->zero) {
         RG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * pl->nbins * nseg, s));
         return RG_OK;
+      }
+      if (moments_selected(pl, nseg)) {
+        RG_TRY(moments_begin(pl, nseg, s));
+        RG_TRY(moments_deposit(pl, comp, d_off, n_single, nseg, s));
+        return moments_finish(pl, nseg, out, s);
+      }
+      if (pl->algo == RG_ALGO_MOMENTS) {
+        return set_error(RG_ERR_UNSUPPORTED, "this plan or run cannot use the interval-moment algorithm");
       }
       RG_TRY(plan_reserve(pl, nseg));
       const int64_t* d_prefix = nullptr;
@@ -960,6 +999,7 @@ int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {
   cudaFree(pl->d_partials);
   cudaFree(pl->d_prefix);
   cudaFree(pl->d_plain_acc);
+  rg::moments_free(pl);
   for (auto* v : { &pl->ev_used, &pl->ev_free }) {
     for (auto& e : *v) {
       cudaEventDestroy(e.first);
@@ -1014,6 +1054,22 @@ int rg_spectrum_plan_probe_stage_timeout(rg_spectrum_plan* pl, uint32_t polls, v
   return RG_OK;
 }
 
+int rg_spectrum_plan_set_algorithm(rg_spectrum_plan* pl, int32_t algo) {
+  if (!pl || (algo != RG_ALGO_AUTO && algo != RG_ALGO_DIRECT && algo != RG_ALGO_MOMENTS)) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_set_algorithm: bad arguments");
+  }
+  pl->algo = algo;
+  return RG_OK;
+}
+
+int rg_spectrum_plan_algorithm(const rg_spectrum_plan* pl, int32_t nseg, int32_t* algo) {
+  if (!pl || !algo || nseg < 1) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_algorithm: bad arguments");
+  }
+  *algo = rg::moments_selected(pl, nseg) ? RG_ALGO_MOMENTS : RG_ALGO_DIRECT;
+  return RG_OK;
+}
+
 int rg_spectrum_plan_enable_timing(rg_spectrum_plan* pl, int32_t enable) {
   if (!pl) {
     return rg::set_error(RG_ERR_ARGUMENT, "null plan");
@@ -1045,6 +1101,7 @@ int rg_spectrum_plan_kernel_time(rg_spectrum_plan* pl, double* ms, int64_t* laun
 }
 
 int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
   if (!plan || (!out && plan->nbins > 0)) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run: null argument");
   }
@@ -1060,6 +1117,7 @@ int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* 
 
 int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
                             int32_t nseg, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
   if (!plan || !offsets || nseg < 0 || (!out && nseg > 0 && plan->nbins > 0)) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_batched: null argument");
   }
@@ -1070,6 +1128,7 @@ int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p, const
 }
 
 int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
   if (!pl || (!out && pl->nbins > 0) || pl->source != rg::kSrcParticles) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_host: bad arguments");
   }
@@ -1096,7 +1155,14 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
   // earlier call on this device, by any plan, or never): the first copies of this call
   // wait for exactly that, so they overlap the tail of the previous call's kernels
   std::lock_guard<std::mutex> lock(st->mu);
-  const int64_t               n = p->n;
+  const int64_t               n       = p->n;
+  const bool                  moments = rg::moments_selected(pl, 1);
+  if (!moments && pl->algo == RG_ALGO_MOMENTS) {
+    return rg::set_error(RG_ERR_UNSUPPORTED, "this plan cannot use the interval-moment algorithm");
+  }
+  if (moments) {
+    RG_TRY(rg::moments_begin(pl, 1, s));
+  }
   for (int64_t a = 0; a < n; a += kStageChunk) {
     const int     b = static_cast<int>(st->issued++ % kBuffers);
     const int64_t m = std::min(kStageChunk, n - a);
@@ -1112,8 +1178,15 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
     }
     RG_CUDA_TRY(cudaEventRecord(st->copied[b], st->copy_stream));
     RG_CUDA_TRY(cudaStreamWaitEvent(s, st->copied[b], 0));
-    RG_TRY(rg::run_fused_chunk(pl, dev, m, a > 0, s));
+    if (moments) {
+      RG_TRY(rg::moments_deposit(pl, dev, nullptr, m, 1, s));
+    } else {
+      RG_TRY(rg::run_fused_chunk(pl, dev, m, a > 0, s));
+    }
     RG_CUDA_TRY(cudaEventRecord(st->consumed[b], s));
+  }
+  if (moments) {
+    return rg::moments_finish(pl, 1, out, s);
   }
   // the rows the chunks accumulated: as many blocks as the first (largest) chunk used
   const int64_t first = std::min(kStageChunk, n);
@@ -1122,6 +1195,7 @@ int rg_spectrum_run_host(rg_spectrum_plan* pl, const rg_particles* p, float* out
 
 int rg_spectrum_run_plain(const rg_spectrum_plan* cplan, const rg_particles* p, float* out,
                           void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
   auto* plan = const_cast<rg_spectrum_plan*>(cplan);
   if (!plan || plan->source != rg::kSrcParticles || plan->table_mode != RG_TABLE_REFERENCE) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_plain: needs a reference-table particle plan");
@@ -1208,6 +1282,7 @@ int rg_synchrotron_spectrum(const rg_particles* p, const float* bins, int32_t nb
 
 int rg_dist_run(const rg_spectrum_plan* plan, const float* gbeta, const float* f, int32_t ng, float* out,
                 void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumFromDist");
   if (!plan || plan->source != rg::kSrcDist || ng < 0 || (ng > 0 && (!gbeta || !f)) ||
       (!out && plan->nbins > 0)) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_dist_run: bad arguments");
@@ -1223,6 +1298,7 @@ int rg_dist_run(const rg_spectrum_plan* plan, const float* gbeta, const float* f
 int rg_synchrotron_spectrum_from_dist(const float* gbeta, const float* f, int32_t ng,
                                       int32_t log_spaced, const float* bins, int32_t nbins,
                                       float g_syn, float e_syn_at_g_syn, float* out, void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumFromDist");
   rg::clear_error();
   if (ng < 0 || nbins < 0 || (ng > 0 && (!gbeta || !f)) || (nbins > 0 && !out)) {
     return rg::set_error(RG_ERR_ARGUMENT, "rg_synchrotron_spectrum_from_dist: bad arguments");

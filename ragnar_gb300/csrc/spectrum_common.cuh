@@ -119,8 +119,10 @@ namespace rg {
     return o;
   }
 
-  // round(S (ln X1 + ln X2)), S = Sh + Sl; the exponent part goes through the
-  // integer constant Cfx = round(S ln2 2^16).
+  // round(S (ln X1 + ln X2) 2^(16 - kShift)), S = Sh + Sl; the exponent part goes
+  // through the integer constant Cfx = round(S ln2 2^16).  kShift = 16 gives the
+  // coordinate in units of S; smaller shifts keep 16 - kShift more fraction bits.
+  template <int kShift = 16>
   __device__ __forceinline__ int64_t fixed_log_sum(ff X1, ff X2, float Sh, float Sl, int64_t Cfx) {
     const LnParts a = ln_parts(X1);
     const LnParts b = ln_parts(X2);
@@ -131,7 +133,7 @@ namespace rg {
     const float pl  = __fadd_rn(pe, __fmaf_rn(s.hi, Sl, __fmul_rn(s.lo, Sh)));
     const int64_t q = static_cast<int64_t>(a.e + b.e) * Cfx + __float2ll_rn(__fmul_rn(ph, 65536.0f)) +
                       __float2ll_rn(__fmul_rn(pl, 65536.0f));
-    return (q + 32768) >> 16;
+    return (q + (int64_t(1) << (kShift - 1))) >> kShift;
   }
 
   // gamma^2 = 1 + u^2 and W = |gamma E + u x B|^2 - (u.E)^2 as double-floats, so
@@ -180,6 +182,29 @@ namespace rg {
     }
     q32 = static_cast<uint32_t>(Q);
     A   = p.amp * sqrtf(__fdiv_rn(W.hi, G.hi));
+    if (p.has_w) {
+      A *= v[9];
+    }
+    return isfinite(A);
+  }
+
+  // The particle stage of the interval-moment path: the same kinematics and amplitude
+  // as particle_stage, with the table coordinate kept to 8 more fraction bits
+  // (Q in units of 2^-(frac + 8) table segments, as a 64-bit integer); the particle
+  // adds nothing unless Pmin - L < Q <= Pmax in those units.
+  __device__ __forceinline__ bool particle_stage_fine(const float (&v)[kComps], const FusedParams& p,
+                                                      int64_t Pmin, int64_t Pmax, int64_t L, int64_t& Q,
+                                                      float& A) {
+    ff G, W;
+    kinematics_ff(v, p.has_e != 0, G, W);
+    if (!(W.hi > 0.0f) || !isfinite(W.hi) || !isfinite(G.hi)) {
+      return false;
+    }
+    Q = fixed_log_sum<8>(G, W, p.Sh, p.Sl, p.Cfx);
+    if (Q <= Pmin - L || Q > Pmax) {
+      return false;
+    }
+    A = p.amp * sqrtf(__fdiv_rn(W.hi, G.hi));
     if (p.has_w) {
       A *= v[9];
     }

@@ -39,6 +39,20 @@ struct rg_spectrum_plan {
   double*               d_plain_acc = nullptr;
   const rg::RefTable*   ref         = nullptr;
   const rg::SmoothTable* smooth     = nullptr;
+  // interval-moment path (reference table, particle source; moments.cu)
+  int                   algo        = RG_ALGO_AUTO;
+  bool                  moments_ok  = false;  // the plan's bins were prepared for it
+  std::vector<int32_t>  h_mslice;             // per slice: (valid bins, cells, histogram offset lo, hi)
+  int32_t*              d_mslice    = nullptr;
+  int64_t*              d_mrange    = nullptr; // per slice: (Pmin, Pmax) in the finer coordinate
+  int64_t               mom_L       = 0;       // table segments in the finer coordinate
+  int32_t*              d_thr       = nullptr; // per slice: sorted low parts of Pmax - P_b (kSliceBins)
+  uint16_t*             d_bucket    = nullptr; // per slice: first threshold of each bucket (kMomBuckets + 1)
+  int4*                 d_binfo     = nullptr; // per bin: (sorted position, cell offset, low part, valid)
+  double2*              d_mcoef     = nullptr; // per table segment: FP64 (c0, c1 per fraction bit)
+  int64_t               hist_per_seg = 0;      // double2 entries of one segment's histograms
+  double2*              d_hist      = nullptr;
+  size_t                hist_cap    = 0;       // double2 entries
   // kernel timing (events bracketing each fused launch)
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
@@ -56,5 +70,15 @@ namespace rg {
   int fill_params(const rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off,
                   const int64_t* d_prefix, int64_t n_single, int nseg, FusedParams& fp);
   int item_prefix(rg_spectrum_plan* pl, const int64_t* d_off, int nseg, int64_t n, cudaStream_t s);
+
+  // Interval-moment path of reference-table particle plans (moments.cu).
+  int  moments_prepare(rg_spectrum_plan* pl, const std::vector<uint8_t>& valid, double ln_xmin, double dln,
+                       double ln_k0);
+  bool moments_selected(const rg_spectrum_plan* pl, int nseg);
+  int  moments_begin(rg_spectrum_plan* pl, int nseg, cudaStream_t s);
+  int  moments_deposit(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
+                       int nseg, cudaStream_t s);
+  int  moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s);
+  void moments_free(rg_spectrum_plan* pl);
 
 } // namespace rg
