@@ -11,11 +11,17 @@ as one batched launch over two segments; protons use e_syn_at_g_syn / 1836.
 Inputs are generated on the device from fixed seeds (synthetic; positions are
 not an input of the spectrum and are not generated).
 
-Reported: evals/s = particles x bins per second (value: device-resident inputs;
-e2e: host-resident pinned inputs through rg_spectrum_run_host, H2D of the inputs
-and D2H of the spectra inside the timed region every step, steps pipelined; the
-step-synchronous figure beside it), the fused kernel's roofline, the CPU baseline,
-clocks.
+Reported: evals/s = particles x bins of spectrum produced per second (value:
+device-resident inputs; e2e: host-resident pinned inputs through
+rg_spectrum_run_host, H2D of the inputs and D2H of the spectra inside the timed
+region every step, steps pipelined; the step-synchronous figure and a copy-only /
+kernel-only breakdown beside it).  The plans sum by interval moments (the default
+for reference-table particle plans): one particle stage per particle deposits FP64
+moments per (table cell, bin interval), then a scan and a per-bin reduce; the
+roofline is that of the deposit kernel (HBM: 28 algorithmic bytes per particle).
+The fused per-eval kernel (every particle x bin pair in FP32) runs the same step
+as a side case with its FP32-issue roofline.  Also: per-species error of the
+headline spectra against the FP64 oracle, the CPU baseline, clocks.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -44,7 +50,8 @@ N_PER_SPECIES = 33_000_000
 NBINS = 512
 BIN_LO, BIN_HI = 1e-4, 1e9
 PROTON_MASS_RATIO = 1836.0
-OPS_PER_EVAL = 6  # IADD, SHF, LOP, LDS.64, FFMA (F), FFMA (accumulate)
+OPS_PER_EVAL = 6  # fused kernel: IADD, SHF, LOP, LDS.64, FFMA (F), FFMA (accumulate)
+BYTES_PER_PARTICLE = 28  # u (12 B), B (12 B), w (4 B), FP32 SoA, read once per deposit
 
 
 def parse_args():
@@ -60,12 +67,14 @@ def parse_args():
                          "IC, the drop-in module calls)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
-    ap.add_argument("--profile-case", nargs="?", const="spectrum", choices=["spectrum", "spectrum200", "smooth", "gemm", "histogram", "ic"],
+    ap.add_argument("--profile-case", nargs="?", const="spectrum",
+                    choices=["spectrum", "spectrum200", "smooth", "gemm", "histogram", "ic", "moments"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
                          "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
                          "energyDistribution of 3.3e7 particles into 200 log bins, 4 calls; 'ic' = "
-                         "ICSpectrum 1024 x 1024 x 1024, 4 calls")
+                         "ICSpectrum 1024 x 1024 x 1024, 4 calls; 'moments' = one 2^24-particle species "
+                         "x 512 bins by interval moments, 4 runs (deposit, scan, reduce)")
     return ap.parse_args()
 
 
@@ -309,22 +318,23 @@ def workload_config():
 # our arm
 # ---------------------------------------------------------------------------------------
 
-def traffic_per_particle():
-    """DRAM bytes per particle of the fused kernel from the committed ncu summary."""
+def profile_value(key):
+    """A figure from the committed ncu summaries (a line '- key: value')."""
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", open(path).read())
+        m = re.search(r"(?m)^- " + re.escape(key) + r":\s*([0-9.eE+-]+)", open(path).read())
         if m:
             return float(m.group(1))
     return None
+
+
+def traffic_per_particle():
+    """DRAM bytes per particle of the fused kernel from the committed ncu summary."""
+    return profile_value("dram_bytes_per_particle")
 
 
 def wavefronts_per_eval():
     """Shared-memory wavefronts per eval of the fused kernel from the committed ncu summary."""
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        m = re.search(r"shared_wavefronts_per_eval:\s*([0-9.eE+-]+)", open(path).read())
-        if m:
-            return float(m.group(1))
-    return None
+    return profile_value("shared_wavefronts_per_eval")
 
 
 def run_ours(args, rank, world, local_rank):
@@ -359,7 +369,7 @@ def run_ours(args, rank, world, local_rank):
         plan_p.run(prt_p, out_p, stream)
 
     evals_per_step = NSPECIES * n_per * NBINS
-    launches_per_step = 5  # item prefix + fused + reduce (e+-), fused + reduce (p)
+    launches_per_step = 6  # deposit + scan + reduce, for the e+- batch and for the protons
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -395,30 +405,9 @@ def run_ours(args, rank, world, local_rank):
     parity = guarded(headline_parity, torch, capi, comps, n_per, bins, plan_e, plan_p, stream) \
         if rank == 0 else None
 
-    # fused-kernel roofline: FP32-core issue slots (SMs x 128 lanes x clock)
-    kern_ms = (ke_ms + kp_ms) / max(ke_n + kp_n, 1)
-    evals_per_launch = evals_per_step / 2.0
-    achieved = OPS_PER_EVAL * evals_per_launch / (kern_ms / 1e3) / 1e12
+    # deposit-kernel roofline: HBM, 28 algorithmic bytes per particle (u, B, w read once)
     clk = clocks.get("sm_mhz") or 2070.0
-    peak = sms * 128 * clk * 1e6 / 1e12
-    tpp = traffic_per_particle()
-    roofline = {
-        "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Top/s",
-        "frac": achieved / peak, "kernel": "fused_spectrum_kernel<16>",
-        "kernel_ms_per_launch": kern_ms, "evals_per_launch": evals_per_launch,
-        "peak_basis": f"{sms} SMs x 128 lanes x median SM clock {clk:.0f} MHz sampled during the "
-                      f"timed region (issue slots; no measured FP32 peak is available)",
-        "traffic": None if tpp is None else tpp * evals_per_launch / NBINS,
-    }
-    wpe = wavefronts_per_eval()
-    if wpe:
-        # the other limit the kernel runs against: the shared-memory data path (one
-        # wavefront per SM-clock) at the table-lookup wavefronts per eval ncu measured
-        lsu_peak = sms * clk * 1e6 / wpe
-        roofline["secondary"] = {
-            "bound": "shared-memory wavefronts", "achieved": evals_per_launch / (kern_ms / 1e3),
-            "peak": lsu_peak, "unit": "evals/s", "frac": evals_per_launch / (kern_ms / 1e3) / lsu_peak,
-            "basis": f"{sms} SMs x {clk:.0f} MHz / {wpe} wavefronts per eval (ncu, committed summary)"}
+    roofline = deposit_roofline(ke_ms + kp_ms, ke_n + kp_n, NSPECIES * n_per, sms, clk)
 
     result = {
         "metric": METRIC, "value": world * evals_per_step / t_step, "unit": UNIT, "n_gpus": world,
@@ -432,6 +421,8 @@ def run_ours(args, rank, world, local_rank):
         result["parity_vs_fp64"] = parity
     extra = {"spectra_finite": spectra_ok}
     if rank == 0 and not args.no_extras:
+        extra["fused_per_eval_same_step"] = guarded(fused_same_step, torch, plan_e, plan_p, step, stream, sms,
+                                                    evals_per_step, max(args.steps // 2, 3))
         extra["energy_distribution_dump"] = guarded(histogram_case, torch, capi, device, comps, NSPECIES * n_per)
         extra["dropin_module_3.3e7"] = guarded(dropin_module_case, torch, comps, n_per)
     # e2e: host-resident pinned inputs through the C ABI, copies inside the timed region
@@ -558,6 +549,79 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(result), flush=True)
 
 
+def deposit_roofline(ms_total, launches, particles_per_step, sms, clk_mhz):
+    """HBM roofline of the interval-moment deposit kernel over the timed steps: 28
+    algorithmic bytes per particle (u, B, w read once) against the measured copy
+    bandwidth; the secondary line is its instruction issue rate (thread instructions
+    per particle from the committed ncu summary) against SMs x 128 lanes x clock."""
+    ms = ms_total / max(launches, 1)
+    steps = max(launches, 1) / 2.0  # two deposits per step: the e+- batch and the protons
+    bytes_per_launch = BYTES_PER_PARTICLE * particles_per_step / 2.0
+    achieved = BYTES_PER_PARTICLE * particles_per_step * steps / (ms_total / 1e3) / 1e9
+    peak, src = measured_peak("hbm_gbs", 6800.0)
+    dbp = profile_value("moments_dram_bytes_per_particle")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": src, "kernel": "moments_deposit_kernel", "kernel_ms_per_launch": ms,
+            "bytes_per_launch": bytes_per_launch,
+            "bytes_basis": f"{BYTES_PER_PARTICLE} B per particle (u, B, w, FP32) x particles per launch",
+            "traffic": None if dbp is None else dbp * particles_per_step / 2.0}
+    ipp = profile_value("moments_thread_inst_per_particle")
+    if ipp:
+        rate = ipp * particles_per_step * steps / (ms_total / 1e3)
+        issue_peak = sms * 128 * clk_mhz * 1e6
+        roof["secondary"] = {"bound": "instruction issue", "achieved": rate / 1e12, "peak": issue_peak / 1e12,
+                             "unit": "T thread-instructions/s", "frac": rate / issue_peak,
+                             "basis": f"{ipp} thread instructions per particle (ncu, committed summary) vs "
+                                      f"{sms} SMs x 128 lanes x {clk_mhz:.0f} MHz"}
+    return roof
+
+
+def fused_same_step(torch, plan_e, plan_p, step, stream, sms, evals_per_step, k):
+    """The headline step with the fused per-eval kernel (every particle x bin pair in
+    FP32): evals/s and its FP32-issue roofline (6 FP32-pipe ops per eval against SMs x
+    128 lanes x clock), the measure the per-eval design is bound by."""
+    for p in (plan_e, plan_p):
+        p.set_algorithm(1)
+    try:
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        plan_e.enable_timing(True)
+        plan_p.enable_timing(True)
+        sampler = ClockSampler(torch.cuda.current_device())
+        sampler.start()
+        t = timed(torch, step, k, warm=0)
+        clocks = sampler.stop()
+        ke_ms, ke_n = plan_e.kernel_time()
+        kp_ms, kp_n = plan_p.kernel_time()
+        plan_e.enable_timing(False)
+        plan_p.enable_timing(False)
+        plan_e.check(stream)
+        plan_p.check(stream)
+    finally:
+        for p in (plan_e, plan_p):
+            p.set_algorithm(0)
+    kern_ms = (ke_ms + kp_ms) / max(ke_n + kp_n, 1)
+    evals_per_launch = evals_per_step / 2.0
+    clk = clocks.get("sm_mhz") or 2070.0
+    achieved = OPS_PER_EVAL * evals_per_launch / (kern_ms / 1e3) / 1e12
+    peak = sms * 128 * clk * 1e6 / 1e12
+    out = {"evals_per_s": evals_per_step / t, "ms_per_step": t * 1e3, "kernel_ms_per_launch": kern_ms,
+           "clocks": clocks,
+           "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Top/s",
+                        "frac": achieved / peak, "kernel": "fused_spectrum_kernel<16>",
+                        "basis": f"{OPS_PER_EVAL} FP32-pipe ops per eval vs {sms} SMs x 128 lanes x "
+                                 f"{clk:.0f} MHz"}}
+    wpe = wavefronts_per_eval()
+    if wpe:
+        lsu_peak = sms * clk * 1e6 / wpe
+        out["roofline_shared_memory"] = {
+            "bound": "shared-memory wavefronts", "achieved": evals_per_launch / (kern_ms / 1e3),
+            "peak": lsu_peak, "unit": "evals/s", "frac": evals_per_launch / (kern_ms / 1e3) / lsu_peak,
+            "basis": f"{sms} SMs x {clk:.0f} MHz / {wpe} wavefronts per eval (ncu, committed summary)"}
+    return out
+
+
 def step_stats(ts):
     """Mean, median and 95th percentile of per-step wall times, in ms."""
     s = sorted(ts)
@@ -677,7 +741,7 @@ def wavefront_roofline(achieved, evals_per_sm_clock, sms, clk_mhz, basis):
 
 def add_wavefront_rooflines(extra, sms, clk_mhz):
     """Roofline fractions of the batched forward and of the forward + adjoint pair."""
-    bg = extra.get("batched_graph_256_segments", {})
+    bg = extra.get("batched_graph_256_segments", {}).get("fused", {})
     if "graph_evals_per_s" in bg:
         bg["roofline"] = wavefront_roofline(
             bg["graph_evals_per_s"], 8.0, sms, clk_mhz,
@@ -751,6 +815,8 @@ def side_measurements(torch, capi, device, stream):
     prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
     plan = capi.SpectrumPlan(photon_bins(), 1.0, 1.0, 1.0)
     o = torch.empty(NBINS, device=device)
+    out["dump_species_8e6_moments_evals_per_s"] = n * NBINS / timed(torch, lambda: plan.run(prt, o, stream), 10)
+    plan.set_algorithm(capi.RG_ALGO_DIRECT)
     out["dump_species_8e6_fused_evals_per_s"] = n * NBINS / timed(torch, lambda: plan.run(prt, o, stream), 10)
     out["dump_species_8e6_plain_evals_per_s"] = n * NBINS / timed(torch, lambda: plan.run_plain(prt, o, stream), 2)
     plan.close()
@@ -762,6 +828,8 @@ def side_measurements(torch, capi, device, stream):
     prt1 = capi.particles(u1, b=[z, z, torch.ones(n1, device=device)], n=n1)
     plan1 = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 200), 1.0, 1.0, 1.0)
     o1 = torch.empty(200, device=device)
+    out["config1_moments_evals_per_s"] = n1 * 200 / timed(torch, lambda: plan1.run(prt1, o1, stream), 20)
+    plan1.set_algorithm(capi.RG_ALGO_DIRECT)
     out["config1_fused_evals_per_s"] = n1 * 200 / timed(torch, lambda: plan1.run(prt1, o1, stream), 20)
     out["config1_plain_evals_per_s"] = n1 * 200 / timed(torch, lambda: plan1.run_plain(prt1, o1, stream), 5)
     plan1.close()
@@ -785,7 +853,15 @@ def batched_graph_case(torch, capi, device):
                           index=torch.repeat_interleave(index, counts))
     bz = torch.ones(total, device=device)
     prt = capi.particles(u, b=[None, None, bz], n=total)
+    res = {"segments": nseg, "particles": total, "photon_bins": nb}
+    for algo, name in ((capi.RG_ALGO_MOMENTS, "moments"), (capi.RG_ALGO_DIRECT, "fused")):
+        res[name] = batched_graph_algo(torch, capi, device, prt, offs, u, bz, nseg, nb, total, algo)
+    return res
+
+
+def batched_graph_algo(torch, capi, device, prt, offs, u, bz, nseg, nb, total, algo):
     plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, nb), 1.0, 1.0, 1.0)
+    plan.set_algorithm(algo)
     plan.reserve(nseg)
     out = torch.empty((nseg, nb), device=device)
     side = torch.cuda.Stream(device)
@@ -800,7 +876,7 @@ def batched_graph_case(torch, capi, device):
     t_graph = timed(torch, graph.replay, 10)
     ref = out.clone()
     t_eager = timed(torch, lambda: plan.run_batched(prt, offs, nseg, out, stream), 10)
-    same = bool(torch.equal(out, ref))
+    same = bool(torch.allclose(out, ref, rtol=2e-7, atol=0.0))
     host_offs = offs.cpu().tolist()
     segs = [capi.particles([c[a:b] for c in u], b=[None, None, bz[a:b]], n=b - a)
             for a, b in zip(host_offs[:-1], host_offs[1:])]
@@ -813,11 +889,11 @@ def batched_graph_case(torch, capi, device):
     plan.check(stream)
     plan.close()
     evals = total * nb
-    return {"segments": nseg, "particles": total, "photon_bins": nb,
-            "graph_evals_per_s": evals / t_graph, "graph_ms": t_graph * 1e3,
+    return {"graph_evals_per_s": evals / t_graph, "graph_ms": t_graph * 1e3,
             "eager_batched_evals_per_s": evals / t_eager,
             "one_launch_per_segment_evals_per_s": evals / t_loop,
-            "graph_equals_eager": same}
+            "graph_matches_eager": same,
+            "match": "bit-identical for the fused kernel; within FP32 rounding for interval moments"}
 
 
 def fwd_adjoint_case(torch, capi, device):
@@ -1119,6 +1195,7 @@ def profile_case():
     n = 1 << 22
     comps = make_particles(torch, n, 1, device, seed=3)
     plan = capi.SpectrumPlan(photon_bins(), 1.0, 1.0, 1.0)
+    plan.set_algorithm(capi.RG_ALGO_DIRECT)
     out = torch.empty(NBINS, device=device)
     prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
     flush = torch.empty(64 << 20, device=device)
@@ -1129,6 +1206,29 @@ def profile_case():
     plan.check()
     plan.close()
     print("profile case done")
+
+
+def profile_case_moments():
+    """4 runs of the interval-moment path (deposit, scan, reduce) on 2^24 particles of
+    the dump-scale e- species x 512 bins (inputs 470 MB, above the L2)."""
+    import torch  # noqa: PLC0415
+
+    from ragnar_gb300 import capi  # noqa: PLC0415
+
+    device = torch.device("cuda", 0)
+    capi.check(capi.lib().rg_init(0))
+    n = 1 << 24
+    comps = make_particles(torch, n, 1, device, seed=3)
+    plan = capi.SpectrumPlan(photon_bins(), 1.0, 1.0, 1.0)
+    assert plan.algorithm(1) == capi.RG_ALGO_MOMENTS
+    out = torch.empty(NBINS, device=device)
+    prt = capi.particles(comps[0:3], b=comps[3:6], w=comps[6], n=n)
+    for _ in range(4):
+        plan.run(prt, out, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    plan.check()
+    plan.close()
+    print("profile case (interval moments) done")
 
 
 def profile_case_200():
@@ -1145,6 +1245,7 @@ def profile_case_200():
     u = config1_particles(torch, n, gen, device)
     prt = capi.particles(u, b=[None, None, torch.ones(n, device=device)], n=n)
     plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 200), 1.0, 1.0, 1.0)
+    plan.set_algorithm(capi.RG_ALGO_DIRECT)
     out = torch.empty(200, device=device)
     flush = torch.empty(64 << 20, device=device)
     for _ in range(4):
@@ -1226,6 +1327,9 @@ def main():
     args = parse_args()
     if args.profile_case == "spectrum":
         profile_case()
+        return
+    if args.profile_case == "moments":
+        profile_case_moments()
         return
     if args.profile_case == "spectrum200":
         profile_case_200()

@@ -188,29 +188,6 @@ namespace rg {
     return isfinite(A);
   }
 
-  // The particle stage of the interval-moment path: the same kinematics and amplitude
-  // as particle_stage, with the table coordinate kept to 8 more fraction bits
-  // (Q in units of 2^-(frac + 8) table segments, as a 64-bit integer); the particle
-  // adds nothing unless Pmin - L < Q <= Pmax in those units.
-  __device__ __forceinline__ bool particle_stage_fine(const float (&v)[kComps], const FusedParams& p,
-                                                      int64_t Pmin, int64_t Pmax, int64_t L, int64_t& Q,
-                                                      float& A) {
-    ff G, W;
-    kinematics_ff(v, p.has_e != 0, G, W);
-    if (!(W.hi > 0.0f) || !isfinite(W.hi) || !isfinite(G.hi)) {
-      return false;
-    }
-    Q = fixed_log_sum<8>(G, W, p.Sh, p.Sl, p.Cfx);
-    if (Q <= Pmin - L || Q > Pmax) {
-      return false;
-    }
-    A = p.amp * sqrtf(__fdiv_rn(W.hi, G.hi));
-    if (p.has_w) {
-      A *= v[9];
-    }
-    return isfinite(A);
-  }
-
   // Per-"particle" stage of a tabulated distribution (synchrotron.hpp:76-94):
   // e_peak = K0 gbeta^2, amplitude f * (gbeta if the gamma bins are log-spaced).
   __device__ __forceinline__ bool dist_stage(float gb, float f, const FusedParams& p, int64_t Pmin,
