@@ -35,7 +35,7 @@
 // (FP64 moments and coefficients) instead of being rounded to FP32 per eval.
 // The FP64 atomic sums make the result independent of the particle order up to
 // FP64 rounding, not bit for bit.
-#include "spectrum_common.cuh"
+#include "moments_common.cuh"
 #include "spectrum_plan.hpp"
 
 #include <algorithm>
@@ -70,161 +70,6 @@ namespace rg {
       double2*        hist;    // nseg x per_seg interval moments (M0, M1)
       int64_t         per_seg;
     };
-
-    __device__ __forceinline__ float rcp_approx(float x) {
-      float r;
-      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-      return r;
-    }
-
-    // ln x = e ln2 + h + l of a positive finite double-float, as ln_parts computes it
-    // (2 atanh((m - 1)/(m + 1)) of the mantissa m in [0.71, 1.42)), with the quotient
-    // taken through one approximate reciprocal: its low part comes from the residual
-    // f - q d, so an approximate q costs nothing in the double-float result (the
-    // residual's own rounding is below 2^-48 absolute).
-    __device__ __forceinline__ LnParts ln_parts_rcp(ff x) {
-      int adj = 0;
-      if (x.hi < 1.17549435e-38f) { // subnormal: scale into the normal range (exact)
-        x.hi = __fmul_rn(x.hi, 0x1p64f);
-        x.lo = __fmul_rn(x.lo, 0x1p64f);
-        adj  = -64;
-      }
-      const uint32_t bits = __float_as_uint(x.hi);
-      int            e    = static_cast<int>(bits >> 23) - 126 + adj; // x.hi = m 2^e, m in [0.5, 1)
-      float          m    = __uint_as_float((bits & 0x007fffffu) | 0x3f000000u);
-      if (m < 0.70710678f) {
-        m = __fmul_rn(m, 2.0f);
-        e -= 1;
-      }
-      const float f  = __fsub_rn(m, 1.0f); // exact
-      const ff    d  = two_sum(m, 1.0f);
-      const float ri = rcp_approx(d.hi);
-      const float q  = __fmul_rn(f, ri);
-      const float r  = __fmaf_rn(-q, d.hi, f);
-      const float zl = __fmul_rn(__fmaf_rn(-q, d.lo, r), ri);
-      const float w  = __fmul_rn(q, q);
-      const float poly =
-        w * (0.33333334f + w * (0.2f + w * (0.14285715f + w * (0.11111111f + w * 0.09090909f))));
-      LnParts o;
-      o.e = e;
-      o.h = __fmul_rn(2.0f, q);
-      o.l = __fadd_rn(__fmaf_rn(o.h, poly, __fmul_rn(2.0f, zl)), __fmul_rn(x.lo, rcp_approx(x.hi)));
-      return o;
-    }
-
-    // GB300 issues FP64 arithmetic and 64-bit conversions at a small fraction of the FP32
-    // rate, so the deposit builds its FP64 values and 64-bit integers with integer
-    // instructions only.
-
-    // round(x) as a 64-bit integer for a finite float x with |x| < 2^62.
-    __device__ __forceinline__ int64_t float_to_ll_rn(float x) {
-      if (fabsf(x) < 4194304.0f) { // |x| < 2^22: round through the 1.5 2^23 shifter
-        return static_cast<int64_t>(__float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000);
-      }
-      const uint32_t b = __float_as_uint(x); // |x| >= 2^22: a multiple of 1/2 ... integral from 2^23
-      const int      E = static_cast<int>((b >> 23) & 0xffu);
-      const uint64_t m = static_cast<uint64_t>((b & 0x7fffffu) | 0x800000u);
-      int64_t        v;
-      if (E >= 150) {
-        v = static_cast<int64_t>(m << (E - 150));
-      } else { // 2^22 <= |x| < 2^23: one fraction bit, round half away from zero
-        v = static_cast<int64_t>((m + 1) >> 1);
-      }
-      return (b >> 31) ? -v : v;
-    }
-
-    // The bits of the double equal to a positive normal float.
-    __device__ __forceinline__ double float_to_double_bits(float a) {
-      const uint32_t b = __float_as_uint(a);
-      const uint64_t d = (static_cast<uint64_t>((b >> 23) + 896u) << 52) | (static_cast<uint64_t>(b & 0x7fffffu) << 29);
-      return __longlong_as_double(static_cast<long long>(d));
-    }
-
-    // a r as a double for a positive normal float a and an integer 0 <= r < 2^30: the
-    // 24-bit mantissa times r is an exact integer below 2^54, rounded to 53 bits.
-    __device__ __forceinline__ double product_to_double_bits(float a, uint32_t r) {
-      if (r == 0) {
-        return 0.0;
-      }
-      const uint32_t b   = __float_as_uint(a);
-      const uint64_t P   = static_cast<uint64_t>((b & 0x7fffffu) | 0x800000u) * r;
-      int            top = 63 - __clzll(static_cast<long long>(P)); // leading bit position, <= 53
-      uint64_t       mant;
-      if (top <= 52) {
-        mant = P << (52 - top);
-      } else { // 54 significant bits: round to nearest (ties up)
-        mant = (P + 1) >> 1;
-        if (mant >> 53) {
-          mant >>= 1;
-          ++top;
-        }
-      }
-      // value = P 2^(E - 150) with E the float's biased exponent
-      const int64_t e = static_cast<int64_t>(top) + static_cast<int64_t>((b >> 23) & 0xffu) - 150 + 1023;
-      const uint64_t d = (static_cast<uint64_t>(e) << 52) | (mant & ((uint64_t(1) << 52) - 1));
-      return __longlong_as_double(static_cast<long long>(d));
-    }
-
-    // The particle stage of this path: the kinematics and amplitude of particle_stage,
-    // with the table coordinate Q = round(2^(kFrac + 8) (ln gamma + ln sqrt W) / dln)
-    // as a 64-bit integer (8 more fraction bits than the fused kernel's).  ln G + ln W
-    // is one logarithm of the product G W wherever that is a normal float.  The particle
-    // adds nothing unless Pmin - L < Q <= Pmax.
-    __device__ __forceinline__ bool moment_particle_stage(const float (&v)[kComps], const FusedParams& p,
-                                                          int64_t Pmin, int64_t Pmax, int64_t L, int64_t& Q,
-                                                          float& A) {
-      ff G, W;
-      kinematics_ff(v, p.has_e != 0, G, W);
-      if (!(W.hi > 0.0f) || !isfinite(W.hi) || !isfinite(G.hi)) {
-        return false;
-      }
-      const ff X = ff_mul(G, W);
-      int      e;
-      ff       s;
-      if (X.hi >= 1.17549435e-38f && X.hi <= 3.0e38f) {
-        const LnParts a = ln_parts_rcp(X);
-        e               = a.e;
-        s               = ff { a.h, a.l };
-      } else {
-        const LnParts a = ln_parts_rcp(G);
-        const LnParts b = ln_parts_rcp(W);
-        e               = a.e + b.e;
-        s               = two_sum(a.h, b.h);
-        s.lo            = __fadd_rn(s.lo, __fadd_rn(a.l, b.l));
-      }
-      const float   ph = __fmul_rn(s.hi, p.Sh);
-      const float   pe = __fmaf_rn(s.hi, p.Sh, -ph);
-      const float   pl = __fadd_rn(pe, __fmaf_rn(s.hi, p.Sl, __fmul_rn(s.lo, p.Sh)));
-      const int64_t q  = static_cast<int64_t>(e) * p.Cfx + float_to_ll_rn(__fmul_rn(ph, 65536.0f)) +
-                        float_to_ll_rn(__fmul_rn(pl, 65536.0f));
-      Q = (q + 128) >> 8;
-      if (Q <= Pmin - L || Q > Pmax) {
-        return false;
-      }
-      // W / G within an ulp (approximate reciprocal and one correction), then sqrt
-      const float rg = rcp_approx(G.hi);
-      float       t  = __fmul_rn(W.hi, rg);
-      t              = __fmaf_rn(__fmaf_rn(-t, G.hi, W.hi), rg, t);
-      A              = p.amp * sqrtf(t);
-      if (p.has_w) {
-        A *= v[9];
-      }
-      return isfinite(A);
-    }
-
-    // Largest s in [0, nseg] with off[s] <= i (off non-decreasing).
-    __device__ __forceinline__ int segment_of(const int64_t* off, int nseg, int64_t i) {
-      int lo = 0, hi = nseg;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (off[mid] <= i) {
-          lo = mid;
-        } else {
-          hi = mid - 1;
-        }
-      }
-      return lo;
-    }
 
     __global__ void __launch_bounds__(kMomThreads) moments_deposit_kernel(const __grid_constant__ MomentParams m) {
       __shared__ int32_t  thr[kSliceBins];
@@ -301,10 +146,10 @@ namespace rg {
           continue;
         }
         double2* h = base + seg * m.per_seg + static_cast<int64_t>(Rc) * row + lo;
-        if (A >= 1.17549435e-38f) {
+        if (fabsf(A) >= 1.17549435e-38f) { // amplitudes may be negative (negative weights or B0)
           atomicAdd(&h->x, float_to_double_bits(A));
           atomicAdd(&h->y, product_to_double_bits(A, Rl));
-        } else if (A > 0.0f) { // subnormal amplitude (rare): the FP64 pipe
+        } else if (A != 0.0f) { // subnormal amplitude (rare): the FP64 pipe
           atomicAdd(&h->x, static_cast<double>(A));
           atomicAdd(&h->y, static_cast<double>(A) * static_cast<double>(Rl));
         }

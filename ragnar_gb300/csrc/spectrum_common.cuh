@@ -280,6 +280,57 @@ namespace rg {
     }
   }
 
+  // dL/dw and dL/du of one particle from R1 = sum_b G_b e_b F(x_pb) and
+  // R2 = sum_b G_b e_b dF/dln x (x_pb), G_b = dL/dS_b (FP32, recomputed kinematics):
+  //   dL/dw = chiR R1,  dL/du = A (R1 d ln chiR / du - R2 d ln e_peak / du).
+  __device__ __forceinline__ void particle_gradient(const float (&v)[kComps], const FusedParams& p,
+                                                    float R1, float R2, float& gw, float (&gu)[3]) {
+    gw = 0.0f;
+    gu[0] = gu[1] = gu[2] = 0.0f;
+    const float u[3] = { v[0], v[1], v[2] };
+    const float E[3] = { v[3], v[4], v[5] };
+    const float B[3] = { v[6], v[7], v[8] };
+    const float G    = fmaf(u[0], u[0], fmaf(u[1], u[1], fmaf(u[2], u[2], 1.0f)));
+    const float c[3] = { ff_diff_of_products(u[1], B[2], u[2], B[1]).hi,
+                         ff_diff_of_products(u[2], B[0], u[0], B[2]).hi,
+                         ff_diff_of_products(u[0], B[1], u[1], B[0]).hi };
+    float       V[3], gW[3], W;
+    if (p.has_e) {
+      const float gamma = sqrtf(G);
+      const float uE    = u[0] * E[0] + u[1] * E[1] + u[2] * E[2];
+      for (int d = 0; d < 3; ++d) {
+        V[d] = fmaf(gamma, E[d], c[d]);
+      }
+      W              = V[0] * V[0] + V[1] * V[1] + V[2] * V[2] - uE * uE;
+      const float VE = V[0] * E[0] + V[1] * E[1] + V[2] * E[2];
+      const float BxV[3] = { B[1] * V[2] - B[2] * V[1], B[2] * V[0] - B[0] * V[2],
+                             B[0] * V[1] - B[1] * V[0] };
+      for (int d = 0; d < 3; ++d) {
+        gW[d] = 2.0f * VE / gamma * u[d] + 2.0f * BxV[d] - 2.0f * uE * E[d];
+      }
+    } else {
+      W = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+      const float Bxc[3] = { B[1] * c[2] - B[2] * c[1], B[2] * c[0] - B[0] * c[2],
+                             B[0] * c[1] - B[1] * c[0] };
+      for (int d = 0; d < 3; ++d) {
+        gW[d] = 2.0f * Bxc[d];
+      }
+    }
+    if (!(W > 0.0f) || !isfinite(W)) {
+      return;
+    }
+    const float chi = p.amp * sqrtf(W / G);
+    const float w   = p.has_w ? v[9] : 1.0f;
+    const float A   = chi * w;
+    const float iW = 0.5f / W, iG = 1.0f / G;
+    for (int d = 0; d < 3; ++d) {
+      const float dlnchi = gW[d] * iW - u[d] * iG;
+      const float dlneps = u[d] * iG + gW[d] * iW;
+      gu[d]              = A * (R1 * dlnchi - R2 * dlneps);
+    }
+    gw = chi * R1;
+  }
+
   // Smooth-table segments staged in shared memory with the cubic's coefficients
   // rescaled to the variable tau' = fraction bits * 2^-23 (tau = tau' 2^(23 - frac),
   // frac in [12, 22]): c1 s, c2 s^2, c3 s^3 with s = 2^(23 - frac), all exact.

@@ -128,3 +128,27 @@ def test_more_segments_than_staged_fall_back_to_fused(gpu, oracle_lib, table):
     got = out.cpu().numpy()
     for s in (0, 1, 517, nseg - 1):
         assert max_rel(got[s], truth[s]) <= SPECTRUM_RTOL
+
+
+@pytest.mark.parametrize("B0,eps,negw", [(1.0, 1.0, True), (-2.0, -1.5, False)])
+def test_negative_amplitudes(gpu, oracle_lib, table, B0, eps, negw):
+    """Negative weights, or B0 and e_syn_at_g_syn both negative (K0 > 0, amplitude
+    1/B0 < 0): every particle still adds its (signed) term, as in the reference's sum."""
+    P = particles(30000, seed=88, bfield="iso", weights=True)
+    if negw:
+        P["w"][::3] *= -1.0
+    bins = oracle_lib.logspace(0.01, 1e7, 200)
+    T, prt = _device(P, gpu)
+    res = {}
+    for algo in (capi.RG_ALGO_DIRECT, capi.RG_ALGO_MOMENTS):
+        plan = capi.SpectrumPlan(bins, B0, 1.0, eps)
+        plan.set_algorithm(algo)
+        out = torch.empty(200, device=gpu)
+        plan.run(prt, out)
+        plan.check()
+        res[algo] = out.cpu().numpy().astype(np.float64)
+    truth = oracle_lib.sync_spectrum_f64(P, bins, B0, 1.0, eps, table)
+    scale = np.abs(truth).max()
+    for algo, got in res.items():
+        # signed sums can cancel: compare against the largest magnitude
+        assert np.max(np.abs(got - truth)) <= SPECTRUM_RTOL * scale, algo
