@@ -42,11 +42,11 @@ enum {
   RG_TABLE_SMOOTH    = 1  /* exact F on a fine log grid, C1 cubic Hermite (differentiable) */
 };
 
-/* How a reference-table particle plan sums its spectrum (rg_spectrum_plan_set_algorithm). */
+/* How a particle plan sums its spectrum (rg_spectrum_plan_set_algorithm). */
 enum {
-  RG_ALGO_AUTO    = 0, /* interval moments where the plan supports them, else the fused kernel */
-  RG_ALGO_DIRECT  = 1, /* the fused kernel: every (particle, bin) pair evaluated in FP32 */
-  RG_ALGO_MOMENTS = 2  /* interval moments: exact FP64 sums per (table cell, bin interval) */
+  RG_ALGO_AUTO    = 0, /* moments where the plan supports them, else the fused kernels */
+  RG_ALGO_DIRECT  = 1, /* the fused kernels: every (particle, bin) pair evaluated in FP32 */
+  RG_ALGO_MOMENTS = 2  /* FP64 moments per table cell (and bin interval) */
 };
 
 /* --------------------------------------------------------------------------
@@ -184,17 +184,30 @@ int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p,
 int rg_spectrum_run_host(rg_spectrum_plan* plan, const rg_particles* p, float* out,
                          void* stream);
 
-/* Chooses how a reference-table particle plan sums its spectrum: RG_ALGO_AUTO
- * (the default: interval moments when the plan supports them, the fused kernel
- * otherwise), RG_ALGO_DIRECT (the fused kernel, which evaluates every (particle,
- * bin) pair in FP32 and is bit-reproducible) or RG_ALGO_MOMENTS (fails with
- * RG_ERR_UNSUPPORTED at run time where the plan cannot take it: smooth table,
- * distribution source, more than 1024 segments).  Both compute the reference's
- * sum over particles and bins of synchrotron.hpp:145-172; interval moments sum
- * the piecewise-linear F exactly in FP64 per (table cell, bin interval), with
- * FP64 atomics (independent of particle order to FP64 rounding).  No reference
- * counterpart. */
+/* Chooses how a particle plan sums its spectrum (and, for the smooth table, its
+ * adjoint): RG_ALGO_AUTO (the default: moments when the plan supports them, the
+ * fused kernels otherwise), RG_ALGO_DIRECT (the fused kernels, which evaluate
+ * every (particle, bin) pair in FP32 and are bit-reproducible) or
+ * RG_ALGO_MOMENTS (fails with RG_ERR_UNSUPPORTED at run time where the plan
+ * cannot take it: smooth table over bins that are not log-uniform, distribution
+ * source, more than 1024 segments).  All compute the reference's sum over
+ * particles and bins of synchrotron.hpp:145-172.  Reference table: interval
+ * moments sum the piecewise-linear F exactly in FP64 per (table cell, bin
+ * interval).  Smooth table over log-uniform bins: four FP64 moments per cell of
+ * the plan's bin-aligned table, and the adjoint as one cubic per cell.  Moments
+ * use FP64 atomics (independent of particle order to FP64 rounding).  No
+ * reference counterpart. */
 int rg_spectrum_plan_set_algorithm(rg_spectrum_plan* plan, int32_t algo);
+/* The smooth table a RG_TABLE_SMOOTH plan evaluates: its segment count, ln of its
+ * first node and segment width in ln x, and (coef: 4 floats per segment, may be
+ * NULL) the cubic Hermite coefficients (c0, c1, c2, c3) in the position tau inside
+ * a segment.  For log-uniform photon bins a plan builds its own table, with nodes
+ * aligned to the bins and a segment width of (bin spacing) / m, m a whole number,
+ * near the device-wide table's ln(1e8) / 2048, covering at least [1e-6, 100];
+ * otherwise it shares the device-wide table (rg_smooth_table).  Extension: the
+ * reference has no differentiable table. */
+int rg_spectrum_plan_smooth_table(const rg_spectrum_plan* plan, float* coef, int32_t* nseg, double* ln_xmin,
+                                  double* dln);
 /* The algorithm a run over `nseg` segments would use (RG_ALGO_DIRECT or RG_ALGO_MOMENTS). */
 int rg_spectrum_plan_algorithm(const rg_spectrum_plan* plan, int32_t nseg, int32_t* algo);
 

@@ -88,6 +88,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_plan_enable_timing": [_vp, _i32],
         "rg_spectrum_plan_set_algorithm": [_vp, _i32],
         "rg_spectrum_plan_algorithm": [_vp, _i32, ctypes.POINTER(_i32)],
+        "rg_spectrum_plan_smooth_table": [_vp, _vp, ctypes.POINTER(_i32), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)],
         "rg_spectrum_plan_kernel_time": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64)],
         "rg_synchrotron_spectrum": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp, _vp],
         "rg_synchrotron_spectrum_noalloc": [ctypes.POINTER(Particles), _vp, _i32, _f32, _f32, _f32, _vp,
@@ -217,6 +219,18 @@ class SpectrumPlan:
     def set_algorithm(self, algo: int) -> None:
         """RG_ALGO_AUTO, RG_ALGO_DIRECT (the fused per-eval kernel) or RG_ALGO_MOMENTS."""
         check(lib().rg_spectrum_plan_set_algorithm(self.handle, algo))
+
+    def smooth_table(self):
+        """(coef [nseg, 4] float32, ln_xmin, dln) of the smooth table this plan evaluates."""
+        import numpy as np  # noqa: PLC0415
+
+        nseg = _i32()
+        lnx, dln = ctypes.c_double(), ctypes.c_double()
+        check(lib().rg_spectrum_plan_smooth_table(self.handle, None, ctypes.byref(nseg), ctypes.byref(lnx),
+                                                  ctypes.byref(dln)))
+        coef = np.empty((nseg.value, 4), np.float32)
+        check(lib().rg_spectrum_plan_smooth_table(self.handle, coef.ctypes.data, None, None, None))
+        return coef, lnx.value, dln.value
 
     def algorithm(self, nseg: int = 1) -> int:
         """The algorithm a run over nseg segments would use."""

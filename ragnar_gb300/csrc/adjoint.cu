@@ -239,7 +239,7 @@ namespace rg {
                                  cudaStream_t s) {
       static std::atomic<uint64_t> configured { 0 };
       const cudaError_t            e = ensure_max_dynamic_smem(
-        adjoint_kernel<K, MODE>, static_cast<int>(adjoint_smem(MODE, kSmoothSegments, kComps)), configured);
+        adjoint_kernel<K, MODE>, static_cast<int>(adjoint_smem(MODE, kSmoothMaxSegments, kComps)), configured);
       if (e != cudaSuccess) {
         return e;
       }
@@ -268,6 +268,12 @@ namespace rg {
                     cudaStream_t s) {
       if (nseg <= 0) {
         return RG_OK;
+      }
+      if (!pl->zero && pl->nbins > 0 && pl->aligned && moments_selected(pl, nseg)) {
+        return smooth_moments_adjoint(pl, comp, d_off, n_single, nseg, grad_out, gw, gu, s);
+      }
+      if (pl->algo == RG_ALGO_MOMENTS && pl->table_mode == kModeSmooth) {
+        return set_error(RG_ERR_UNSUPPORTED, "this plan or run cannot use the moment adjoint");
       }
       if (pl->nslices != 1) {
         return set_error(RG_ERR_UNSUPPORTED, "the adjoint supports up to 512 photon bins");
@@ -318,7 +324,7 @@ namespace rg {
           return RG_OK;
         }
       }
-      const size_t smem = adjoint_smem(pl->table_mode, kSmoothSegments, nslots);
+      const size_t smem = adjoint_smem(pl->table_mode, fp.hseg, nslots);
       const cudaError_t e = (pl->table_mode == kModeRef)
                               ? launch_adjoint_mode<kModeRef>(pl->K, fp, x, G, smem, s)
                               : launch_adjoint_mode<kModeSmooth>(pl->K, fp, x, G, smem, s);

@@ -245,17 +245,24 @@ namespace rg {
   }
 
   int build_smooth_table(SmoothTable& t, cudaStream_t s) {
-    t.ln_xmin = std::log(kSmoothXmin);
-    t.dln     = std::log(kSmoothXmax / kSmoothXmin) / kSmoothSegments;
+    return build_smooth_table_geom(t, std::log(kSmoothXmin), std::log(kSmoothXmax / kSmoothXmin) / kSmoothSegments,
+                                   kSmoothSegments, s);
+  }
+
+  int build_smooth_table_geom(SmoothTable& t, double ln_xmin, double dln, int nseg, cudaStream_t s) {
+    if (nseg < 1 || nseg > kSmoothMaxSegments || !(dln > 0.0)) {
+      return set_error(RG_ERR_ARGUMENT, "smooth table: bad geometry");
+    }
+    t.ln_xmin = ln_xmin;
+    t.dln     = dln;
+    t.nseg    = nseg;
     ScratchBuffer<double2> nodes;
-    RG_CUDA_TRY(cudaMalloc(&nodes.p, sizeof(double2) * (kSmoothSegments + 1)));
-    RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float4) * (kSmoothSegments + 1)));
-    RG_CUDA_TRY(cudaMemsetAsync(t.d_coef + kSmoothSegments, 0, sizeof(float4), s));
-    smooth_nodes_kernel<<<(kSmoothSegments + 1 + 127) / 128, 128, 0, s>>>(kSmoothSegments + 1,
-                                                                           t.ln_xmin, t.dln, nodes.p);
+    RG_CUDA_TRY(cudaMalloc(&nodes.p, sizeof(double2) * (nseg + 1)));
+    RG_CUDA_TRY(cudaMalloc(&t.d_coef, sizeof(float4) * (nseg + 1)));
+    RG_CUDA_TRY(cudaMemsetAsync(t.d_coef + nseg, 0, sizeof(float4), s));
+    smooth_nodes_kernel<<<(nseg + 1 + 127) / 128, 128, 0, s>>>(nseg + 1, t.ln_xmin, t.dln, nodes.p);
     RG_CUDA_TRY(cudaGetLastError());
-    smooth_coef_kernel<<<(kSmoothSegments + 127) / 128, 128, 0, s>>>(nodes.p, kSmoothSegments, t.dln,
-                                                                     t.d_coef);
+    smooth_coef_kernel<<<(nseg + 127) / 128, 128, 0, s>>>(nodes.p, nseg, t.dln, t.d_coef);
     RG_CUDA_TRY(cudaGetLastError());
     RG_CUDA_TRY(cudaStreamSynchronize(s));
     return RG_OK;

@@ -279,6 +279,9 @@ namespace rg {
   int moments_prepare(rg_spectrum_plan* pl, const std::vector<uint8_t>& valid, double ln_xmin, double dln,
                       double ln_k0) {
     pl->moments_ok = false;
+    if (pl->table_mode == kModeSmooth && pl->aligned) {
+      return smooth_moments_prepare(pl, ln_k0);
+    }
     if (pl->table_mode != kModeRef || pl->source != kSrcParticles || pl->ref->n - 1 > kMomMaxTable) {
       return RG_OK;
     }
@@ -391,6 +394,9 @@ namespace rg {
   // the interval moments.
   int moments_deposit(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off, int64_t n,
                       int nseg, cudaStream_t s) {
+    if (pl->aligned) {
+      return smooth_moments_deposit(pl, comp, d_off, n, nseg, s);
+    }
     MomentParams m {};
     fill_params(pl, comp, nullptr, nullptr, n, 1, m.fp);
     m.range   = pl->d_mrange;
@@ -432,6 +438,9 @@ namespace rg {
 
   // Prefix sums of the moments and the per-bin sums into out (nseg x nbins).
   int moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s) {
+    if (pl->aligned) {
+      return smooth_moments_finish(pl, nseg, out, s);
+    }
     const int warps = 8;
     moments_scan_kernel<<<dim3((max_cells(pl) + warps - 1) / warps, nseg * pl->nslices), 32 * warps, 0, s>>>(
       pl->d_hist, reinterpret_cast<const int4*>(pl->d_mslice), pl->nslices, pl->hist_per_seg);
@@ -460,6 +469,10 @@ namespace rg {
     cudaFree(pl->d_binfo);
     cudaFree(pl->d_mcoef);
     cudaFree(pl->d_hist);
+    cudaFree(pl->d_alpha);
+    cudaFree(pl->own_smooth.d_coef);
+    pl->d_alpha           = nullptr;
+    pl->own_smooth.d_coef = nullptr;
     pl->d_mslice = nullptr;
     pl->d_mrange = nullptr;
     pl->d_thr    = nullptr;

@@ -95,6 +95,9 @@ namespace rg {
 
   // Smooth (differentiable) table: exact F on a log grid, cubic Hermite segments.
   constexpr int    kSmoothSegments = 2048;
+  // Upper bound on the segments of any smooth table (the device-wide one above or a
+  // plan's own table aligned to its bins); sizes the kernels' shared-memory limit.
+  constexpr int    kSmoothMaxSegments = 4096;
   constexpr double kSmoothXmin     = 1e-6;
   constexpr double kSmoothXmax     = 100.0;
 
@@ -109,8 +112,9 @@ namespace rg {
   };
 
   struct SmoothTable {
-    float4* d_coef  = nullptr; // kSmoothSegments (c0, c1, c2, c3) in tau, then one zero entry
+    float4* d_coef  = nullptr; // nseg (c0, c1, c2, c3) in tau, then one zero entry
     double  ln_xmin = 0, dln = 0;
+    int     nseg    = kSmoothSegments;
   };
 
   // Device staging for host-resident particle streams.  Every host-input call on a
@@ -151,6 +155,8 @@ namespace rg {
   // Builds the reference table on `n` nodes of Logspace(xmin, xmax) (FP64 on the GPU).
   int build_reference_table(int n, float xmin, float xmax, RefTable& t, cudaStream_t s);
   int build_smooth_table(SmoothTable& t, cudaStream_t s);
+  // A smooth table of nseg segments of width dln (in ln x) from ln_xmin.
+  int build_smooth_table_geom(SmoothTable& t, double ln_xmin, double dln, int nseg, cudaStream_t s);
   // Makes the allocation-free entry point's scratch array and kernels resident on `dev`
   // (the current device) and builds its F table; noalloc.cu.
   int noalloc_prepare(int dev);

@@ -187,7 +187,7 @@ int rg_smooth_table(float* coef, int32_t* nseg, double* ln_xmin, double* dln) {
   const rg::SmoothTable* t = nullptr;
   RG_TRY(rg::smooth_table(&t));
   if (nseg) {
-    *nseg = rg::kSmoothSegments;
+    *nseg = t->nseg;
   }
   if (ln_xmin) {
     *ln_xmin = t->ln_xmin;
@@ -196,7 +196,7 @@ int rg_smooth_table(float* coef, int32_t* nseg, double* ln_xmin, double* dln) {
     *dln = t->dln;
   }
   if (coef) {
-    RG_CUDA_TRY(cudaMemcpy(coef, t->d_coef, sizeof(float4) * rg::kSmoothSegments, cudaMemcpyDeviceToHost));
+    RG_CUDA_TRY(cudaMemcpy(coef, t->d_coef, sizeof(float4) * t->nseg, cudaMemcpyDeviceToHost));
   }
   return RG_OK;
 }

@@ -536,7 +536,7 @@ namespace rg {
     cudaError_t configure_fused_k() {
       static std::atomic<uint64_t> configured { 0 };
       return ensure_max_dynamic_smem(fused_spectrum_kernel<K, MODE>,
-                                     static_cast<int>(fused_smem(MODE, kSmoothSegments, kComps)), configured);
+                                     static_cast<int>(fused_smem(MODE, kSmoothMaxSegments, kComps)), configured);
     }
 
     template <int K, int MODE>
@@ -712,7 +712,7 @@ namespace rg {
       } else {
         ln_xmin = pl->smooth->ln_xmin;
         dln     = pl->smooth->dln;
-        nseg    = kSmoothSegments;
+        nseg    = pl->smooth->nseg;
       }
     }
 
@@ -794,7 +794,7 @@ namespace rg {
     fp.amp         = pl->amp;
     fp.table       = pl->ref->d_coef;
     fp.htable      = pl->smooth ? pl->smooth->d_coef : nullptr;
-    fp.hseg        = kSmoothSegments;
+    fp.hseg        = pl->smooth ? pl->smooth->nseg : kSmoothSegments;
     fp.frac        = pl->frac;
     fp.partials    = pl->d_partials;
     fp.nslices     = pl->nslices;
@@ -910,7 +910,7 @@ namespace rg {
       const int G = d_off ? pl->grid : single_segment_grid(pl, n_single);
       const bool any = d_off ? true : n_single > 0;
       if (any) {
-        RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(pl->table_mode, kSmoothSegments, nslots), s));
+        RG_TRY(timed_launch(pl, fp, dim3(G, pl->nslices), fused_smem(pl->table_mode, fp.hseg, nslots), s));
       }
       return reduce_rows(pl, d_prefix, n_single, G, nseg, out, s);
     }
@@ -926,7 +926,7 @@ namespace rg {
       fp.accumulate      = accumulate ? 1 : 0;
       if (n > 0) {
         RG_TRY(timed_launch(pl, fp, dim3(single_segment_grid(pl, n), pl->nslices),
-                            fused_smem(pl->table_mode, kSmoothSegments, nslots), s));
+                            fused_smem(pl->table_mode, fp.hseg, nslots), s));
       }
       return RG_OK;
     }
@@ -972,6 +972,14 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
                     (static_cast<double>(g_syn) * g_syn * static_cast<double>(B0));
   pl->zero = !(K0 > 0.0) || !std::isfinite(K0);
   pl->amp  = static_cast<float>(1.0 / static_cast<double>(B0));
+  if (table_mode == RG_TABLE_SMOOTH && !pl->zero) {
+    // log-uniform bins: the plan's own smooth table aligned to them (moments_smooth.cu)
+    st = rg::smooth_align_plan(pl.get(), std::log(K0));
+    if (st != RG_OK) {
+      rg_spectrum_plan_destroy(pl.release());
+      return st;
+    }
+  }
   double ln_xmin, dln;
   int    nseg;
   rg::table_geometry(pl.get(), ln_xmin, dln, nseg);
@@ -1051,6 +1059,27 @@ int rg_spectrum_plan_probe_stage_timeout(rg_spectrum_plan* pl, uint32_t polls, v
   }
   rg::stage_wait_probe_kernel<<<1, 64, 0, static_cast<cudaStream_t>(stream)>>>(pl->d_status, polls);
   RG_CUDA_TRY(cudaGetLastError());
+  return RG_OK;
+}
+
+int rg_spectrum_plan_smooth_table(const rg_spectrum_plan* pl, float* coef, int32_t* nseg, double* ln_xmin,
+                                  double* dln) {
+  if (!pl || pl->table_mode != RG_TABLE_SMOOTH || !pl->smooth) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_plan_smooth_table: needs a smooth-table plan");
+  }
+  const rg::SmoothTable* t = pl->smooth;
+  if (nseg) {
+    *nseg = t->nseg;
+  }
+  if (ln_xmin) {
+    *ln_xmin = t->ln_xmin;
+  }
+  if (dln) {
+    *dln = t->dln;
+  }
+  if (coef) {
+    RG_CUDA_TRY(cudaMemcpy(coef, t->d_coef, sizeof(float4) * t->nseg, cudaMemcpyDeviceToHost));
+  }
   return RG_OK;
 }
 

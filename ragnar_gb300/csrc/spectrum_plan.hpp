@@ -53,6 +53,13 @@ struct rg_spectrum_plan {
   int64_t               hist_per_seg = 0;      // double2 entries of one segment's histograms
   double2*              d_hist      = nullptr;
   size_t                hist_cap    = 0;       // double2 entries
+  // smooth table aligned to log-uniform bins (moments_smooth.cu)
+  rg::SmoothTable       own_smooth;            // the plan's own table when `aligned`
+  bool                  aligned     = false;
+  int64_t               sm_pmin = 0, sm_pmax = 0; // smallest / largest bin coordinate, fine units
+  int                   sm_cells    = 0;
+  float4*               d_alpha     = nullptr; // adjoint cell cubics, nseg x cells
+  size_t                alpha_cap   = 0;
   // kernel timing (events bracketing each fused launch)
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
@@ -80,5 +87,13 @@ namespace rg {
                        int nseg, cudaStream_t s);
   int  moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s);
   void moments_free(rg_spectrum_plan* pl);
+  // The smooth-table variant (moments_smooth.cu).
+  int  smooth_align_plan(rg_spectrum_plan* pl, double ln_k0);
+  int  smooth_moments_prepare(rg_spectrum_plan* pl, double ln_k0);
+  int  smooth_moments_deposit(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
+                              int nseg, cudaStream_t s);
+  int  smooth_moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s);
+  int  smooth_moments_adjoint(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
+                              int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s);
 
 } // namespace rg
