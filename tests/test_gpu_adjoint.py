@@ -1,8 +1,11 @@
 """The differentiable path: the smooth F table built on the GPU, the smooth-mode
-forward, and the hand-written adjoint kernel behind torch.autograd, checked
-against the FP64 oracle (its own table from std::cyl_bessel_k, its analytic
-gradient) and against FP64 central finite differences (h = 1e-6 relative) of a
-log-space loss on 64 randomly chosen particles."""
+forward, and the adjoint behind torch.autograd, checked against the FP64 oracle
+(its own table from std::cyl_bessel_k, its analytic gradient) and against FP64
+central finite differences (h = 1e-6 relative) of a log-space loss on 64
+randomly chosen particles.  Log-uniform photon bins give a plan its own smooth
+table aligned to the bins; both ways of summing run on it: the fused kernels
+(every particle x bin pair) and the cell moments (forward: four moments per
+table cell; adjoint: one cubic per cell)."""
 
 from __future__ import annotations
 
@@ -42,19 +45,46 @@ def test_smooth_table_matches_independent_oracle(oracle_lib, smooth):
     assert np.max(np.abs(coef[~big] - ref[~big])) < 1e-36
 
 
+ALGOS = [pytest.param(1, id="direct"), pytest.param(2, id="moments")]
+
+
+def plan_table(plan):
+    """(coef, xmin, xmax) of the smooth table a plan evaluates, for the oracle."""
+    coef, lnx, dln = plan.smooth_table()
+    return coef, float(np.exp(lnx)), float(np.exp(lnx + coef.shape[0] * dln))
+
+
+def test_plan_table_matches_independent_oracle(gpu, oracle_lib):
+    """A plan's own (bin-aligned) table against the oracle's FP64 Hermite coefficients
+    on the same geometry; bins that are not log-uniform keep the device-wide table."""
+    plan = rt.spectrum_plan(oracle_lib.logspace(0.01, 1e7, 512))
+    coef, xmin, xmax = plan_table(plan)
+    assert coef.shape[0] != 2048 and xmin <= 1e-6 * (1 + 1e-12) and xmax >= 100.0 * (1 - 1e-12)
+    ref = oracle_lib.smooth_coefficients(coef.shape[0], xmin, xmax)
+    scale = np.abs(ref[:, 0:1]) + np.abs(ref[:, 1:2])
+    big = scale[:, 0] > 1e-30
+    assert np.max(np.abs(coef[big] - ref[big]) / scale[big]) < 3e-7
+    uneven = rt.spectrum_plan(np.array([0.1, 0.3, 2.0, 50.0, 51.0], np.float32))
+    assert uneven.smooth_table()[0].shape[0] == 2048
+    assert uneven.algorithm(1) == capi.RG_ALGO_DIRECT
+    assert plan.algorithm(1) == capi.RG_ALGO_MOMENTS
+
+
 def _device(P, dev):
     return {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in P.items()}
 
 
-@pytest.mark.parametrize("nbins,lo,hi", [(200, 0.01, 1e7), (512, 0.01, 1e7), (77, 1e-3, 1e5)])
-def test_smooth_forward(gpu, oracle_lib, smooth, nbins, lo, hi):
-    coef, _, _ = smooth
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("nbins,lo,hi", [(200, 0.01, 1e7), (512, 0.01, 1e7), (77, 1e-3, 1e5), (1500, 1e-4, 1e9)])
+def test_smooth_forward(gpu, oracle_lib, nbins, lo, hi, algo):
     P = particles(20000, seed=nbins, bfield="iso", weights=True)
     bins = oracle_lib.logspace(lo, hi, nbins)
     T = _device(P, gpu)
     plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
     S = rt.synchrotron_spectrum(plan, T["w"], T["ux"], T["uy"], T["uz"], T["bx"], T["by"], T["bz"])
-    truth = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef)
+    coef, xmin, xmax = plan_table(plan)
+    truth = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
     assert max_rel(S.cpu().numpy(), truth) <= SPECTRUM_RTOL
 
 
@@ -64,14 +94,17 @@ def _log_loss_np(S, St, floor=1e-12):
     return np.sum((np.log(S[m]) - np.log(St[m])) ** 2) / m.sum(), m
 
 
-def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth):
-    coef, _, _ = smooth
+@pytest.mark.parametrize("algo", ALGOS)
+def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, algo):
     n, nbins = 4000, 512
     P = particles(n, seed=21, bfield="iso", weights=True)
     Pt = particles(n, seed=22, bfield="iso", weights=True, index=-2.5, umax=300.0)
     bins = oracle_lib.logspace(0.01, 1e7, nbins)
-    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef)
-    St = oracle_lib.sync_smooth_f64(Pt, bins, 1.0, 1.0, 1.0, coef)
+    plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
+    coef, xmin, xmax = plan_table(plan)
+    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
+    St = oracle_lib.sync_smooth_f64(Pt, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
     L0, m = _log_loss_np(S64, St)
     M = m.sum()
     gS = np.zeros(nbins)
@@ -79,7 +112,6 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
 
     # GPU adjoint driven by the same dL/dS
     T = _device(P, gpu)
-    plan = rt.spectrum_plan(bins)
     prt = capi.particles([T["ux"], T["uy"], T["uz"]], b=[T["bx"], T["by"], T["bz"]], w=T["w"])
     gw = torch.empty(n, device=gpu)
     gu = [torch.empty(n, device=gpu) for _ in range(3)]
@@ -88,7 +120,7 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
     g_gpu = np.stack([gw.cpu().numpy()] + [g.cpu().numpy() for g in gu]).astype(np.float64)
 
     # FP64 analytic gradient of the same function
-    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS)
+    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS, xmin, xmax)
     g64 = np.vstack([gw64[None], gu64])
     scale = np.max(np.abs(g64), axis=1, keepdims=True)
     assert np.max(np.abs(g_gpu - g64) / scale) < 1e-4
@@ -103,7 +135,7 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
     worst = 0.0
     for p in rng.choice(n, 64, replace=False):
         one = {k: P[k][p:p + 1].astype(np.float64) for k in keys}
-        s_p = oracle_lib.sync_smooth_f64(one, bins, 1.0, 1.0, 1.0, coef)
+        s_p = oracle_lib.sync_smooth_f64(one, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
         rest = S64 - s_p
         for c, key in enumerate(("w", "ux", "uy", "uz")):
             x0 = one[key][0]
@@ -112,7 +144,7 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
             for sgn in (1.0, -1.0):
                 q = {k: v.copy() for k, v in one.items()}
                 q[key][0] = x0 + sgn * h
-                s_pm.append(oracle_lib.sync_smooth_f64(q, bins, 1.0, 1.0, 1.0, coef))
+                s_pm.append(oracle_lib.sync_smooth_f64(q, bins, 1.0, 1.0, 1.0, coef, xmin, xmax))
             Sp, Sm = rest + s_pm[0], rest + s_pm[1]
             dlog = np.log1p((s_pm[0] - s_pm[1])[m] / Sm[m])
             fd = np.sum(dlog * (np.log(Sp[m]) + np.log(Sm[m]) - 2.0 * lt)) / M / (2 * h)
@@ -124,8 +156,8 @@ def test_adjoint_vs_fp64_gradient_and_finite_differences(gpu, oracle_lib, smooth
     assert worst < 1e-4, worst
 
 
-def test_autograd_end_to_end(gpu, oracle_lib, smooth):
-    coef, _, _ = smooth
+@pytest.mark.parametrize("algo", ALGOS)
+def test_autograd_end_to_end(gpu, oracle_lib, algo):
     n, nbins = 3000, 256
     P = particles(n, seed=31, bfield="iso", weights=True, efield=True)
     bins = oracle_lib.logspace(0.01, 1e6, nbins)
@@ -133,28 +165,32 @@ def test_autograd_end_to_end(gpu, oracle_lib, smooth):
     for k in ("w", "ux", "uy", "uz"):
         T[k].requires_grad_(True)
     plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
+    coef, xmin, xmax = plan_table(plan)
     S = rt.synchrotron_spectrum(plan, T["w"], T["ux"], T["uy"], T["uz"], T["bx"], T["by"], T["bz"],
                                 T["ex"], T["ey"], T["ez"])
     target = S.detach() * torch.linspace(0.5, 1.5, nbins, device=gpu)
     loss = rt.log_mse(S, target)
     loss.backward()
-    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef)
+    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
     St = S64 * np.linspace(0.5, 1.5, nbins, dtype=np.float32).astype(np.float64)
     _, m = _log_loss_np(S64, St)
     gS = np.zeros(nbins)
     gS[m] = 2.0 * (np.log(S64[m]) - np.log(St[m])) / (m.sum() * S64[m])
-    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS)
+    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS, xmin, xmax)
     for got, want in [(T["w"].grad, gw64)] + [(T[k].grad, gu64[i]) for i, k in enumerate(("ux", "uy", "uz"))]:
         g = got.cpu().numpy()
         assert np.max(np.abs(g - want)) / np.max(np.abs(want)) < 1e-3
 
 
-def test_batched_adjoint_matches_per_segment(gpu, oracle_lib):
+@pytest.mark.parametrize("algo", ALGOS)
+def test_batched_adjoint_matches_per_segment(gpu, oracle_lib, algo):
     P = particles(9000, seed=41, bfield="iso", weights=True)
     bins = oracle_lib.logspace(0.01, 1e7, 128)
     T = _device(P, gpu)
     prt = capi.particles([T["ux"], T["uy"], T["uz"]], b=[T["bx"], T["by"], T["bz"]], w=T["w"])
     plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
     offs = torch.tensor([0, 2000, 2000, 9000], dtype=torch.int64, device=gpu)
     plan.reserve(3)
     gS = torch.rand((3, 128), device=gpu)

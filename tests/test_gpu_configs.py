@@ -17,8 +17,6 @@
 
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -80,23 +78,17 @@ def test_config1_spectrum_and_histogram_at_full_size(gpu, oracle_lib):
     assert int(counts.sum()) == n
 
 
-@pytest.fixture(scope="module")
-def smooth_coef(gpu):
-    nseg = ctypes.c_int32()
-    capi.check(capi.lib().rg_smooth_table(None, ctypes.byref(nseg), None, None))
-    coef = np.empty((nseg.value, 4), np.float32)
-    capi.check(capi.lib().rg_smooth_table(coef.ctypes.data, None, None, None))
-    return coef
-
-
-def test_config4_gradient_at_full_size(gpu, oracle_lib, smooth_coef):
+@pytest.mark.parametrize("algo", [pytest.param(1, id="direct"), pytest.param(2, id="moments")])
+def test_config4_gradient_at_full_size(gpu, oracle_lib, algo):
     n, nbins = 10_000_000, 512
-    coef = smooth_coef
     P = config1_particles(n, seed=4)
     P["w"] = np.ones(n, np.float32)
     Pt = config1_particles(2_000_000, seed=44, index=-2.5, umax=1e4, gcut=300.0)
     bins = oracle_lib.logspace(0.01, 1e7, nbins)
     plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
+    coef, lnx, dln = plan.smooth_table()
+    xmin, xmax = float(np.exp(lnx)), float(np.exp(lnx + coef.shape[0] * dln))
 
     T = {k: torch.from_numpy(v).to(gpu) for k, v in P.items()}
     Tt = {k: torch.from_numpy(v).to(gpu) for k, v in Pt.items()}
@@ -111,14 +103,14 @@ def test_config4_gradient_at_full_size(gpu, oracle_lib, smooth_coef):
     g_gpu = np.stack([T[k].grad.cpu().numpy() for k in ("w", "ux", "uy", "uz")]).astype(np.float64)
 
     # forward and full gradient in FP64 (every particle), driven by the FP64 dL/dS
-    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef)
+    S64 = oracle_lib.sync_smooth_f64(P, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
     assert max_rel(S.detach().cpu().numpy(), S64) <= SPECTRUM_RTOL
     St_np = St.cpu().numpy().astype(np.float64)
     m = (S64 > 1e-12 * S64.max()) & (St_np > 1e-12 * St_np.max())
     M = m.sum()
     gS = np.zeros(nbins)
     gS[m] = 2.0 * (np.log(S64[m]) - np.log(St_np[m])) / (M * S64[m])
-    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS)
+    gw64, gu64 = oracle_lib.sync_smooth_grad_f64(P, bins, 1.0, 1.0, 1.0, coef, gS, xmin, xmax)
     g64 = np.vstack([gw64[None], gu64])
     scale = np.max(np.abs(g64), axis=1, keepdims=True)
     assert np.max(np.abs(g_gpu - g64) / scale) < 1e-4
@@ -131,7 +123,7 @@ def test_config4_gradient_at_full_size(gpu, oracle_lib, smooth_coef):
     worst = 0.0
     for p in rng.choice(n, 64, replace=False):
         one = {k: P[k][p:p + 1].astype(np.float64) for k in keys}
-        s_p = oracle_lib.sync_smooth_f64(one, bins, 1.0, 1.0, 1.0, coef)
+        s_p = oracle_lib.sync_smooth_f64(one, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
         rest = S64 - s_p
         for c, key in enumerate(("w", "ux", "uy", "uz")):
             x0 = one[key][0]
@@ -140,7 +132,7 @@ def test_config4_gradient_at_full_size(gpu, oracle_lib, smooth_coef):
             for sgn in (1.0, -1.0):
                 q = {k: v.copy() for k, v in one.items()}
                 q[key][0] = x0 + sgn * h
-                s_pm.append(oracle_lib.sync_smooth_f64(q, bins, 1.0, 1.0, 1.0, coef))
+                s_pm.append(oracle_lib.sync_smooth_f64(q, bins, 1.0, 1.0, 1.0, coef, xmin, xmax))
             Sp, Sm = rest + s_pm[0], rest + s_pm[1]
             dlog = np.log1p((s_pm[0] - s_pm[1])[m] / Sm[m])
             fd = np.sum(dlog * (np.log(Sp[m]) + np.log(Sm[m]) - 2.0 * lt)) / M / (2 * h)
