@@ -8,7 +8,7 @@
 // For photon bins that are log-uniform (Logbins), a plan builds its own smooth
 // table on a grid aligned to the bins: node spacing dln = (bin spacing) / m for an
 // integer m, and nodes placed so that every bin's table coordinate t_b is an
-// integer up to a tiny residual eps_b (float rounding of the bins; |eps_b| < 1e-4
+// integer up to a tiny residual eps_b (float rounding of the bins; |eps_b| < 1e-3
 // segments).  With x = e_b / e_peak, t = t_b - q_p, q_p = ln e_peak_p / dln, every
 // bin then sees a particle at the same position inside a segment,
 //   tau_p = frac(-q_p),   segment s = t_b - ceil(q_p),
@@ -44,7 +44,10 @@ namespace rg {
     constexpr int    kSmSharedSeg = 1024;      // segment offsets staged in shared memory
     constexpr int    kSmRows      = 16;        // segment groups of the reduce kernel
     constexpr double kTargetDln   = 0.0089954; // ln(1e8) / 2048: the device-wide table's spacing
-    constexpr double kUniformTol  = 1e-4;      // largest bin residual, in table segments
+    // Largest bin residual |eps_b|, in table segments.  Logbins-style bins carry ~2e-6 in
+    // ln e (their exponent is rounded to float before the power); the first-order
+    // correction leaves eps^2 |F''| / 2 < 1e-6 F at this bound.
+    constexpr double kUniformTol  = 1e-3;
 
     struct SmoothMomParams {
       FusedParams    fp;        // streams, kinematics constants (plan's frac), status
