@@ -371,8 +371,7 @@ int rg_spectrum_adjoint_batched(rg_spectrum_plan* plan, const rg_particles* p, c
 int rg_dist_plan_create(const float* bins, int32_t nbins, float g_syn, float e_syn_at_g_syn,
                         int32_t log_spaced, int32_t table_mode, rg_spectrum_plan** plan) {
   // a particle plan with B0 = 1 has K0 = eps / g^2, the distribution's constant
-  RG_TRY(rg_spectrum_plan_create(bins, nbins, 1.0f, g_syn, e_syn_at_g_syn, table_mode, plan));
-  (*plan)->source     = rg::kSrcDist;
+  RG_TRY(rg::create_plan(bins, nbins, 1.0f, g_syn, e_syn_at_g_syn, table_mode, rg::kSrcDist, plan));
   (*plan)->log_spaced = log_spaced ? 1 : 0;
   (*plan)->amp        = 1.0f;
   return RG_OK;

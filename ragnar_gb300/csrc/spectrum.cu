@@ -938,12 +938,10 @@ namespace rg {
 
   } // namespace
 
-} // namespace rg
-
-extern "C" {
-
-int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_syn,
-                            float e_syn_at_g_syn, int32_t table_mode, rg_spectrum_plan** plan) {
+  // A plan for particles or (source kSrcDist) for one tabulated distribution; only particle
+  // plans over log-uniform bins take a bin-aligned smooth table.
+  int create_plan(const float* bins, int32_t nbins, float B0, float g_syn, float e_syn_at_g_syn,
+                  int32_t table_mode, int source, rg_spectrum_plan** plan) {
   rg::clear_error();
   if (!plan) {
     return rg::set_error(RG_ERR_ARGUMENT, "null plan pointer");
@@ -957,7 +955,7 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
   }
   auto pl        = std::make_unique<rg_spectrum_plan>();
   pl->table_mode = table_mode;
-  pl->source     = rg::kSrcParticles;
+  pl->source     = source;
   pl->B0         = B0;
   pl->g_syn      = g_syn;
   pl->eps        = e_syn_at_g_syn;
@@ -972,7 +970,7 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
                     (static_cast<double>(g_syn) * g_syn * static_cast<double>(B0));
   pl->zero = !(K0 > 0.0) || !std::isfinite(K0);
   pl->amp  = static_cast<float>(1.0 / static_cast<double>(B0));
-  if (table_mode == RG_TABLE_SMOOTH && !pl->zero) {
+  if (table_mode == RG_TABLE_SMOOTH && !pl->zero && source == rg::kSrcParticles) {
     // log-uniform bins: the plan's own smooth table aligned to them (moments_smooth.cu)
     st = rg::smooth_align_plan(pl.get(), std::log(K0));
     if (st != RG_OK) {
@@ -993,6 +991,15 @@ int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_
   }
   *plan = pl.release();
   return RG_OK;
+  }
+
+} // namespace rg
+
+extern "C" {
+
+int rg_spectrum_plan_create(const float* bins, int32_t nbins, float B0, float g_syn,
+                            float e_syn_at_g_syn, int32_t table_mode, rg_spectrum_plan** plan) {
+  return rg::create_plan(bins, nbins, B0, g_syn, e_syn_at_g_syn, table_mode, rg::kSrcParticles, plan);
 }
 
 int rg_spectrum_plan_destroy(rg_spectrum_plan* pl) {

@@ -68,6 +68,8 @@ struct rg_spectrum_plan {
 namespace rg {
 
   // Shared plan helpers (spectrum.cu).
+  int  create_plan(const float* bins, int32_t nbins, float B0, float g_syn, float e_syn_at_g_syn,
+                   int32_t table_mode, int source, rg_spectrum_plan** plan);
   int  plan_reserve(rg_spectrum_plan* pl, int max_seg);
   int  check_particles(const rg_particles* p);
   void particle_comps(const rg_particles* p, const float* out[10]);
