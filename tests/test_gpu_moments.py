@@ -44,7 +44,10 @@ def test_algorithm_selection(gpu, oracle_lib):
     assert ref.algorithm(1) == capi.RG_ALGO_DIRECT
     with pytest.raises(capi.RgError):
         ref.set_algorithm(7)
-    smooth = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
+    # smooth table: moments over log-uniform bins (the plan's bin-aligned table) only
+    assert capi.SpectrumPlan(bins, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH).algorithm(1) == capi.RG_ALGO_MOMENTS
+    uneven = np.sort(np.concatenate([bins[:100], bins[100:] * 1.01])).astype(np.float32)
+    smooth = capi.SpectrumPlan(uneven, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
     assert smooth.algorithm(1) == capi.RG_ALGO_DIRECT
     smooth.set_algorithm(capi.RG_ALGO_MOMENTS)
     P = particles(100, seed=1)
