@@ -68,13 +68,16 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--profile-case", nargs="?", const="spectrum",
-                    choices=["spectrum", "spectrum200", "smooth", "gemm", "histogram", "ic", "moments"],
+                    choices=["spectrum", "spectrum200", "smooth", "smooth_moments", "gemm", "histogram", "ic",
+                             "moments"],
                     help="small case for ncu captures, then exit: 'spectrum' = one 4.19e6-particle "
                          "species x 512 bins, 4 fused-kernel launches; 'gemm' = 4096 distributions x "
                          "1024 gamma bins x 1024 photon bins, 4 tcgen05 GEMM launches; 'histogram' = "
                          "energyDistribution of 3.3e7 particles into 200 log bins, 4 calls; 'ic' = "
                          "ICSpectrum 1024 x 1024 x 1024, 4 calls; 'moments' = one 2^24-particle species "
-                         "x 512 bins by interval moments, 4 runs (deposit, scan, reduce)")
+                         "x 512 bins by interval moments, 4 runs (deposit, scan, reduce); 'smooth' / "
+                         "'smooth_moments' = the smooth table, 4 forward + 4 adjoint runs, fused kernels on "
+                         "2^22 particles / cell moments on 2^24 particles")
     return ap.parse_args()
 
 
@@ -540,6 +543,15 @@ def run_ours(args, rank, world, local_rank):
         extra["adam_fit_1024x512x512"] = guarded(adam_fit_case, torch, capi, device)
         extra["ic_1024x1024x1024"] = guarded(ic_case, torch, capi, device, clocks.get("sm_mhz") or 2070.0)
         add_wavefront_rooflines(extra, sms, clocks.get("sm_mhz") or 2070.0)
+        fa = extra["fwd_adjoint_1e7x512"]
+        if "moments" in fa:
+            # the metric's second figure: forward + adjoint of the differentiable spectrum
+            result["fwd_plus_adjoint"] = {
+                "value": fa["moments"]["fwd_plus_adjoint_evals_per_s"], "unit": UNIT,
+                "workload": "1e7 particles x 512 bins 0.01..1e7, smooth table; dL/dw and dL/du",
+                "ms": fa["moments"]["fwd_plus_adjoint_ms"], "roofline": fa["moments"]["roofline"],
+                "fused_per_eval_value": fa["fused"].get("fwd_plus_adjoint_evals_per_s"),
+                "plain_fwd_value": fa["plain_fwd_evals_per_s"]}
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     result["extra"] = extra
@@ -747,7 +759,7 @@ def add_wavefront_rooflines(extra, sms, clk_mhz):
             bg["graph_evals_per_s"], 8.0, sms, clk_mhz,
             "200 bins 0.045 dex apart over 0.040-dex table segments: each 32-lane 8-byte lookup takes 4 "
             "wavefronts (16 lanes touch ~18 distinct entries), so 8 evals per SM-clock")
-    fa = extra.get("fwd_adjoint_1e7x512", {})
+    fa = extra.get("fwd_adjoint_1e7x512", {}).get("fused", {})
     if "fwd_plus_adjoint_evals_per_s" in fa:
         basis = ("smooth table: every lane reads its own 16-byte Hermite segment, at least 4 wavefronts "
                  "per 32 evals in each kernel")
@@ -898,8 +910,10 @@ def batched_graph_algo(torch, capi, device, prt, offs, u, bz, nseg, nb, total, a
 
 def fwd_adjoint_case(torch, capi, device):
     """1e7 particles (|u| ~ u^-2 on [1, 100], isotropic, B = z, w = 1) x 512 bins
-    0.01..1e7 with the smooth (differentiable) table: forward, adjoint, and the
-    plain reference-table kernel on the same particles."""
+    0.01..1e7 with the smooth (differentiable) table, which the plan aligns to these
+    log-uniform bins: forward, adjoint (dL/dw and dL/du) and the pair, by cell moments
+    (the default) and by the fused per-eval kernels, beside the plain reference-table
+    kernel on the same particles."""
     n, nb = 10_000_000, 512
     gen = torch.Generator(device=device).manual_seed(404)
     u = config1_particles(torch, n, gen, device)
@@ -907,30 +921,43 @@ def fwd_adjoint_case(torch, capi, device):
     w = torch.ones(n, device=device)
     prt = capi.particles(u, b=[z, z, torch.ones(n, device=device)], w=w, n=n)
     bins = logbins(capi, 0.01, 1e7, nb)
-    plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
     S = torch.empty(nb, device=device)
     gS = torch.rand(nb, device=device, generator=gen)
     gw = torch.empty(n, device=device)
     gu = [torch.empty(n, device=device) for _ in range(3)]
     stream = torch.cuda.current_stream(device).cuda_stream
-    t_fwd = timed(torch, lambda: plan.run(prt, S, stream), 10)
-    t_adj = timed(torch, lambda: plan.adjoint(prt, gS, gw, gu, stream), 10)
+    evals = n * nb
+    res = {"particles": n, "photon_bins": nb, "table": "smooth, aligned to the bins"}
+    for algo, name in ((capi.RG_ALGO_MOMENTS, "moments"), (capi.RG_ALGO_DIRECT, "fused")):
+        plan = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
+        plan.set_algorithm(algo)
+        t_fwd = timed(torch, lambda: plan.run(prt, S, stream), 10)
+        t_adj = timed(torch, lambda: plan.adjoint(prt, gS, gw, gu, stream), 10)
 
-    def step():
-        plan.run(prt, S, stream)
-        plan.adjoint(prt, gS, gw, gu, stream)
+        def step():
+            plan.run(prt, S, stream)
+            plan.adjoint(prt, gS, gw, gu, stream)
 
-    t_step = timed(torch, step, 10)
-    plan.check(stream)
+        t_step = timed(torch, step, 10)
+        plan.check(stream)
+        plan.close()
+        res[name] = {"fwd_evals_per_s": evals / t_fwd, "adjoint_evals_per_s": evals / t_adj,
+                     "fwd_plus_adjoint_evals_per_s": evals / t_step, "fwd_plus_adjoint_ms": t_step * 1e3,
+                     "fwd_ms": t_fwd * 1e3, "adjoint_ms": t_adj * 1e3}
+    # moments: HBM roofline of the pair (forward reads 28 B per particle, the adjoint
+    # reads 28 B and writes 16 B: dL/dw and dL/du)
+    peak, src = measured_peak("hbm_gbs", 6800.0)
+    mo = res["moments"]
+    gbs = 72.0 * n / (mo["fwd_plus_adjoint_ms"] * 1e-3) / 1e9
+    mo["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                      "peak_source": src,
+                      "basis": "72 algorithmic bytes per particle per forward + adjoint pair (u, B, w read by "
+                               "each; dL/dw and dL/du written)"}
     plain = capi.SpectrumPlan(bins, 1.0, 1.0, 1.0)
     t_plain = timed(torch, lambda: plain.run_plain(prt, S, stream), 3)
     plain.close()
-    plan.close()
-    evals = n * nb
-    return {"particles": n, "photon_bins": nb, "table": "smooth",
-            "fwd_evals_per_s": evals / t_fwd, "adjoint_evals_per_s": evals / t_adj,
-            "fwd_plus_adjoint_evals_per_s": evals / t_step, "fwd_plus_adjoint_ms": t_step * 1e3,
-            "plain_fwd_evals_per_s": evals / t_plain}
+    res["plain_fwd_evals_per_s"] = evals / t_plain
+    return res
 
 
 def fromdist_gemm_case(torch, capi, device, peak_bf16):
@@ -1257,21 +1284,22 @@ def profile_case_200():
     print("profile case (200 bins) done")
 
 
-def profile_case_smooth():
-    """The differentiable path on 2^22 particles (|u| ~ u^-2 on [1, 100], isotropic, B = z,
-    w = 1) x 512 bins 0.01..1e7 with the smooth table: 4 forward and 4 adjoint launches."""
+def profile_case_smooth(algo=1, n=1 << 22):
+    """The differentiable path on n particles (|u| ~ u^-2 on [1, 100], isotropic, B = z,
+    w = 1) x 512 bins 0.01..1e7 with the smooth table: 4 forward and 4 adjoint runs, by
+    the fused kernels (algo 1) or the cell moments (algo 2)."""
     import torch  # noqa: PLC0415
 
     from ragnar_gb300 import capi  # noqa: PLC0415
 
     device = torch.device("cuda", 0)
     capi.check(capi.lib().rg_init(0))
-    n = 1 << 22
     gen = torch.Generator(device=device).manual_seed(5)
     u = config1_particles(torch, n, gen, device)
     w = torch.ones(n, device=device)
     prt = capi.particles(u, b=[None, None, torch.ones(n, device=device)], w=w, n=n)
     plan = capi.SpectrumPlan(logbins(capi, 0.01, 1e7, 512), 1.0, 1.0, 1.0, capi.RG_TABLE_SMOOTH)
+    plan.set_algorithm(algo)
     out = torch.empty(512, device=device)
     gS = torch.rand(512, device=device, generator=gen)
     gw = torch.empty(n, device=device)
@@ -1336,6 +1364,9 @@ def main():
         return
     if args.profile_case == "smooth":
         profile_case_smooth()
+        return
+    if args.profile_case == "smooth_moments":
+        profile_case_smooth(2, 1 << 24)
         return
     if args.profile_case == "gemm":
         profile_gemm_case()
