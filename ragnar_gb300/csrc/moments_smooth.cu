@@ -17,7 +17,7 @@
 // bin, and bin b reads segment Rc - Dc_b (Dc_b = (Pmax >> F) - t_b).  The forward is
 //   S_b / e_b = sum_cells sum_j c'_j(Rc - Dc_b) M_j(Rc),  M_j = sum_p A_p tau_p^j,
 //   c'_j = c_j + eps_b (j + 1) c_{j+1}   (first order in eps_b: F(tau + eps)),
-// four FP64 moments per cell (deposited into 8 sub-cells per cell, which spreads the
+// four FP64 moments per cell (deposited into 32 slots per cell, which spreads the
 // atomics of crowded cells, then folded), and the adjoint of a loss L with
 // G_b = dL/dS_b is, per particle, the cubic of its cell
 //   R1(tau) = sum_b G_b e_b F_b(tau) = sum_j alpha_j(Rc) tau^j,
@@ -38,8 +38,11 @@ namespace rg {
 
   namespace {
 
-    constexpr int    kSub         = 8;         // sub-cells per cell
-    constexpr int    kSubBits     = 3;
+    // Slots per cell: a particle adds its moments (which are absolute within the cell) to
+    // the slot of its lane, shifted by its position in the cell, so the lanes of a warp
+    // whose particles crowd one cell hit different addresses.
+    constexpr int    kSub         = 32;
+    constexpr int    kSubBits     = 5;
     constexpr int    kSmThreads   = 256;
     constexpr int    kSmSharedSeg = 1024;      // segment offsets staged in shared memory
     constexpr int    kSmRows      = 16;        // segment groups of the reduce kernel
@@ -106,7 +109,7 @@ namespace rg {
         const uint64_t R   = static_cast<uint64_t>(m.Pmax - Q);
         const uint32_t Rc  = static_cast<uint32_t>(R >> m.F);
         const uint32_t Rl  = static_cast<uint32_t>(R) & mask;
-        const int      sub = static_cast<int>(Rl >> (m.F - kSubBits));
+        const int      sub = static_cast<int>(((Rl >> (m.F - kSubBits)) + threadIdx.x) & (kSub - 1));
         const int      seg = m.seg_off ? segment_of(soff, m.nseg, i) : 0;
         if (Rc >= static_cast<uint32_t>(m.nc) || seg >= m.nseg) { // self-check: never taken for live particles
           atomicOr(m.fp.status, kDevBadIndex);
