@@ -17,9 +17,8 @@
 // bin, and bin b reads segment Rc - Dc_b (Dc_b = (Pmax >> F) - t_b).  The forward is
 //   S_b / e_b = sum_cells sum_j c'_j(Rc - Dc_b) M_j(Rc),  M_j = sum_p A_p tau_p^j,
 //   c'_j = c_j + eps_b (j + 1) c_{j+1}   (first order in eps_b: F(tau + eps)),
-// four FP64 moments per cell (deposited into 32 slots per cell, laid out slot-major so
-// that the atomics of a crowded cell spread over addresses and L2 slices, then
-// folded), and the adjoint of a loss L with
+// four FP64 moments per cell (deposited into 32 slots per cell, which spreads the
+// atomics of crowded cells, then folded), and the adjoint of a loss L with
 // G_b = dL/dS_b is, per particle, the cubic of its cell
 //   R1(tau) = sum_b G_b e_b F_b(tau) = sum_j alpha_j(Rc) tau^j,
 //   alpha_j(c) = sum_b G_b e_b c'_j(c - Dc_b),   R2 = (dR1/dtau) / dln,
@@ -62,7 +61,7 @@ namespace rg {
       int            nseg;
       int64_t        n;
       int            nc;        // cells
-      double*        hist;      // [nseg][kSub][nc][4]: a cell's slots far apart (different L2 slices)
+      double*        hist;      // [nseg][nc][kSub][4]
     };
 
     // Stages and checks the segment offsets (as the interval-moment deposit does); false
@@ -118,7 +117,7 @@ namespace rg {
         }
         const float tau = __uint2float_rn(Rl) * m.tau_scale;
         const float a1  = A * tau, a2 = a1 * tau, a3 = a2 * tau;
-        double*     h   = m.hist + ((static_cast<int64_t>(seg) * kSub + sub) * m.nc + Rc) * 4;
+        double*     h   = m.hist + ((static_cast<int64_t>(seg) * m.nc + Rc) * kSub + sub) * 4;
         red_add_float(h + 0, A);
         red_add_float(h + 1, a1);
         red_add_float(h + 2, a2);
@@ -126,25 +125,25 @@ namespace rg {
       }
     }
 
-    // Sums each cell's slots into slot 0 (thread per (segment, cell, moment)).
-    __global__ void smooth_fold_kernel(double* hist, int nc, int nseg) {
+    // Sums each cell's sub-cells into sub-cell 0 (thread per (segment, cell, moment)).
+    __global__ void smooth_fold_kernel(double* hist, int64_t cells_total) {
       const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (t >= static_cast<int64_t>(nseg) * nc * 4) {
+      if (t >= cells_total * 4) {
         return;
       }
-      const int64_t seg  = t / (static_cast<int64_t>(nc) * 4);
-      const int64_t rest = t - seg * nc * 4; // cell * 4 + moment
-      double*       h    = hist + seg * kSub * nc * 4 + rest;
+      const int64_t cell = t >> 2;
+      const int     j    = static_cast<int>(t & 3);
+      double*       h    = hist + cell * kSub * 4 + j;
       double        s    = 0.0;
-#pragma unroll 8
+#pragma unroll
       for (int k = 0; k < kSub; ++k) {
-        s += h[static_cast<int64_t>(k) * nc * 4];
+        s += h[k * 4];
       }
       h[0] = s;
     }
 
     struct SmoothReduceParams {
-      const double*   hist; // folded: cell moments in slot 0
+      const double*   hist; // folded: cell moments at sub-cell 0
       int             nc;
       const int4*     binfo; // per bin: (Dc, eps bits, 0, valid)
       const float4*   coef;  // the plan's table, nseg segments
@@ -167,14 +166,14 @@ namespace rg {
       double sum = 0.0;
       if (bi.w) {
         const double  eps = static_cast<double>(__int_as_float(bi.y));
-        const double* h   = r.hist + static_cast<int64_t>(seg) * kSub * r.nc * 4;
+        const double* h   = r.hist + static_cast<int64_t>(seg) * r.nc * kSub * 4;
         for (int s = threadIdx.y; s < r.nseg_tab; s += kSmRows) {
           const int c = bi.x + s;
           if (c >= r.nc) {
             break;
           }
           const float4  k  = __ldg(r.coef + s);
-          const double* M  = h + static_cast<int64_t>(c) * 4;
+          const double* M  = h + static_cast<int64_t>(c) * kSub * 4;
           const double  c0 = k.x, c1 = k.y, c2 = k.z, c3 = k.w;
           sum += (c0 + eps * c1) * M[0] + (c1 + 2.0 * eps * c2) * M[1] + (c2 + 3.0 * eps * c3) * M[2] + c3 * M[3];
         }
@@ -437,7 +436,7 @@ namespace rg {
   int smooth_moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s) {
     const int64_t cells_total = static_cast<int64_t>(nseg) * pl->sm_cells;
     smooth_fold_kernel<<<static_cast<int>((cells_total * 4 + 255) / 256), 256, 0, s>>>(
-      reinterpret_cast<double*>(pl->d_hist), pl->sm_cells, nseg);
+      reinterpret_cast<double*>(pl->d_hist), cells_total);
     RG_CUDA_TRY(cudaGetLastError());
     SmoothReduceParams r {};
     r.hist     = reinterpret_cast<const double*>(pl->d_hist);
