@@ -47,6 +47,7 @@ namespace rg {
     constexpr int    kSmSharedSeg = 1024;      // segment offsets staged in shared memory
     constexpr int    kSmRows      = 16;        // segment groups of the reduce kernel
     constexpr double kTargetDln   = 0.0089954; // ln(1e8) / 2048: the device-wide table's spacing
+    constexpr size_t kSmSharedMax = 200 * 1024; // shared-memory cell table of the block-aggregated deposit
     // Largest bin residual |eps_b|, in table segments.  Logbins-style bins carry ~2e-6 in
     // ln e (their exponent is rounded to float before the power); the first-order
     // correction leaves eps^2 |F''| / 2 < 1e-6 F at this bound.
@@ -122,6 +123,57 @@ namespace rg {
         red_add_float(h + 1, a1);
         red_add_float(h + 2, a2);
         red_add_float(h + 3, a3);
+      }
+    }
+
+    // Single-segment runs whose cell table fits in shared memory: one 1024-thread block per
+    // SM accumulates the four moments of every cell in shared memory (FP64 atomics on the
+    // block's own copy) and adds its copy to slot 0 of the global table once at the end, so
+    // the global atomics are per (block, cell), not per particle.
+    constexpr int kSmSharedThreads = 1024;
+
+    __global__ void __launch_bounds__(kSmSharedThreads, 1)
+      smooth_deposit_shared_kernel(const __grid_constant__ SmoothMomParams m) {
+      extern __shared__ __align__(16) double cellm[]; // nc x 4
+      for (int i = threadIdx.x; i < m.nc * 4; i += blockDim.x) {
+        cellm[i] = 0.0;
+      }
+      if (__syncthreads_or(*m.fp.status != kDevOk)) {
+        return;
+      }
+      const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+      const uint32_t mask   = (1u << m.F) - 1u;
+      for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+        float v[kComps];
+#pragma unroll
+        for (int c = 0; c < kComps; ++c) {
+          v[c] = m.fp.comp[c] ? __ldg(m.fp.comp[c] + i) : 0.0f;
+        }
+        int64_t Q = 0;
+        float   A = 0.0f;
+        if (!moment_particle_stage(v, m.fp, m.Pmin, m.Pmax, m.L, Q, A)) {
+          continue;
+        }
+        const uint64_t R  = static_cast<uint64_t>(m.Pmax - Q);
+        const uint32_t Rc = static_cast<uint32_t>(R >> m.F);
+        if (Rc >= static_cast<uint32_t>(m.nc)) { // self-check: never taken for live particles
+          atomicOr(m.fp.status, kDevBadIndex);
+          continue;
+        }
+        const float tau = __uint2float_rn(static_cast<uint32_t>(R) & mask) * m.tau_scale;
+        const float a1  = A * tau, a2 = a1 * tau, a3 = a2 * tau;
+        double*     h   = cellm + Rc * 4;
+        atomicAdd(h + 0, static_cast<double>(A));
+        atomicAdd(h + 1, static_cast<double>(a1));
+        atomicAdd(h + 2, static_cast<double>(a2));
+        atomicAdd(h + 3, static_cast<double>(a3));
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < m.nc * 4; i += blockDim.x) {
+        const double x = cellm[i];
+        if (x != 0.0) {
+          atomicAdd(m.hist + (static_cast<int64_t>(i >> 2) * kSub) * 4 + (i & 3), x);
+        }
       }
     }
 
@@ -424,7 +476,18 @@ namespace rg {
       }
       RG_CUDA_TRY(cudaEventRecord(ev.first, s));
     }
-    smooth_deposit_kernel<<<grid, kSmThreads, 0, s>>>(m);
+    const size_t cell_bytes = sizeof(double) * 4 * static_cast<size_t>(pl->sm_cells);
+    if (!d_off && cell_bytes <= kSmSharedMax) {
+      static std::atomic<uint64_t> configured { 0 };
+      RG_CUDA_TRY(ensure_max_dynamic_smem(smooth_deposit_shared_kernel, static_cast<int>(kSmSharedMax), configured));
+      DeviceContext* ctx = nullptr;
+      RG_TRY(context(&ctx));
+      const int64_t need = (n + kSmSharedThreads - 1) / kSmSharedThreads;
+      const int     g1   = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, ctx->sms)));
+      smooth_deposit_shared_kernel<<<g1, kSmSharedThreads, cell_bytes, s>>>(m);
+    } else {
+      smooth_deposit_kernel<<<grid, kSmThreads, 0, s>>>(m);
+    }
     RG_CUDA_TRY(cudaGetLastError());
     if (pl->timing) {
       RG_CUDA_TRY(cudaEventRecord(ev.second, s));
