@@ -49,8 +49,8 @@ namespace rg {
   namespace {
 
     constexpr int kMomFrac       = kFrac + 8;        // fraction bits of the coordinate
-    constexpr int kMomBuckets    = 1024;             // buckets over the low kMomFrac bits
-    constexpr int kMomBucketBits = kMomFrac - 10;
+    constexpr int kMomBuckets    = 4096;             // buckets over the low kMomFrac bits
+    constexpr int kMomBucketBits = kMomFrac - 12;
     constexpr int kMomSharedSeg  = 1024;             // segment offsets staged in shared memory
     constexpr int kMomThreads    = 256;
     constexpr int kMomRows       = 16;               // cell groups of the reduce kernel
