@@ -231,3 +231,33 @@ def test_dist_adjoint(gpu, oracle_lib, smooth):
     gf64 = K.T @ w.cpu().numpy().astype(np.float64)
     gf = f_t.grad.cpu().numpy()
     assert np.max(np.abs(gf - gf64)) / np.max(np.abs(gf64)) < 1e-5
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_smooth_host_streaming_matches_device(gpu, oracle_lib, algo):
+    """Host-resident particles of several staging chunks through a smooth plan (its moments
+    accumulate over the chunks) match the same particles resident on the device and the
+    FP64 oracle on the plan's table."""
+    n = (1 << 22) + 3001
+    P = particles(n, seed=61, bfield="iso", weights=True)
+    bins = oracle_lib.logspace(0.01, 1e7, 256)
+    plan = rt.spectrum_plan(bins)
+    plan.set_algorithm(algo)
+    H = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in P.items()}
+    hprt = capi.host_particles([H["ux"], H["uy"], H["uz"]], b=[H["bx"], H["by"], H["bz"]], w=H["w"], n=n)
+    out = torch.empty(256, device=gpu)
+    plan.run_host(hprt, out)
+    T = _device(P, gpu)
+    prt = capi.particles([T["ux"], T["uy"], T["uz"]], b=[T["bx"], T["by"], T["bz"]], w=T["w"])
+    dev = torch.empty(256, device=gpu)
+    plan.run(prt, dev)
+    plan.check()
+    assert max_rel(out.cpu().numpy(), dev.cpu().numpy()) <= 1e-6
+    coef, xmin, xmax = plan_table(plan)
+    sub = {k: v[:200000] for k, v in P.items()}
+    T2 = _device(sub, gpu)
+    prt2 = capi.particles([T2["ux"], T2["uy"], T2["uz"]], b=[T2["bx"], T2["by"], T2["bz"]], w=T2["w"])
+    plan.run(prt2, dev)
+    plan.check()
+    truth = oracle_lib.sync_smooth_f64(sub, bins, 1.0, 1.0, 1.0, coef, xmin, xmax)
+    assert max_rel(dev.cpu().numpy(), truth) <= SPECTRUM_RTOL
