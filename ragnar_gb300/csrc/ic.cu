@@ -15,9 +15,17 @@
 //   KN = p log2 p + ((1 + h) + ((1 - h) / L - log2 L) p - (2 / L^2) p^2),
 // whose quadratic's coefficients depend on (e, g) only and are set once per item.
 // Per eval: FMUL (p = (L t / g) (1 / (4 e_s))), MUFU.LG2, two FFMA (quadratic), FFMA (log
-// term), select of KN (q <= 1, i.e. p <= L), FFMA into the FP32 accumulator.  q >= 1e-30 is
-// guaranteed by a floor on t/g set per (e, g) from the smallest 1 / (4 e_s), so the log's
-// argument is always a normal float.
+// term), max(KN, 0), FFMA into the FP32 accumulator.  max(KN, 0) is KN [q <= 1]: at fixed
+// h, KN(1) = 0, KN'(1) = -1 - h < 0 and KN'' = 2/q - 4 < 0 for q > 1/2, so KN < 0 for every
+// q > 1, while KN >= 0 on (0, 1] (the Klein-Nishina kernel).  Evals with p = inf (masked
+// soft photons; (e, g) pairs that no soft photon reaches, e >= g or an invalid e, which get
+// pg = inf) evaluate to NaN, which max(., 0) also maps to 0.  q >= 1e-30 is guaranteed by a
+// floor on t/g set per (e, g) from the smallest 1 / (4 e_s), so the log's argument is a
+// normal float or inf.  (A form without the per-eval logarithm, log2 p split into
+// log2 (t/g) + log2 (1/(4 e_s)) per item and per photon, takes five FP32 instructions per
+// eval but leaves absolute errors of a few ulp of those logarithms' magnitudes in KN: 2.4e-5
+// to 8.6e-5 from FP64 on the reference's delta-function soft-photon cases, where a single
+// (g, s) pair at 1 - q = 3.5e-3 feeds an IC bin.)
 //
 // Layout: lanes own IC bins (K rows of 32 per lane, 512-bin slices in blockIdx.y); warps take
 // (gamma bin, 64-soft-photon chunk) items; per item the FP32 sums are scaled by
@@ -114,20 +122,21 @@ namespace rg {
           continue; // non-positive or non-finite gamma bins contribute nothing (warp-uniform)
         }
         const float inv_g = __frcp_rn(gv);
-        // per (e, g): t / g, 1 + h, 1 - h; q = (t / g) / (4 e_s) > 1 marks no contribution
+        // per (e, g): pg = L t / g, 1 + h, 1 - h; q = (t / g) / (4 e_s) > 1 marks no
+        // contribution, and so does pg = inf for a pair that no soft photon reaches
         float pg[K], A0[K], B1[K], acc[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
           const float e = energy(k);
           const float d = __fsub_rn(gv, e);
+          const bool  reach = e > 0.0f && d > 0.0f;
           float       t = 0.0f, h = 0.0f;
-          if (e > 0.0f && d > 0.0f) {
+          if (reach) {
             t = __fdiv_rn(e, d);
             h = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(t, t)), __fadd_rn(1.0f, t));
-          } else {
-            t = 3.0e38f; // q = huge: every soft photon fails q <= 1
           }
-          pg[k]  = __fmul_rn(kL, fmaxf(__fmul_rn(t, inv_g), tg_floor)); // p = pg / (4 e_s)
+          pg[k]  = reach ? __fmul_rn(kL, fmaxf(__fmul_rn(t, inv_g), tg_floor)) // p = pg / (4 e_s)
+                         : __int_as_float(0x7f800000);
           A0[k]  = __fadd_rn(1.0f, h);
           B1[k]  = __fsub_rn(__fdiv_rn(__fsub_rn(1.0f, h), kL), kLog2L);
           acc[k] = 0.0f;
@@ -138,12 +147,12 @@ namespace rg {
 #pragma unroll
           for (int k = 0; k < K; ++k) {
             const float pq = __fmul_rn(pg[k], i4);
-            // p >= L 1e-30 by the floor on t/g, so the log's argument is a normal float;
-            // p > L (q > 1) or NaN selects 0 whatever KN evaluated to
+            // p >= L 1e-30 by the floor on t/g, so the log's argument is a normal float or
+            // inf; max(KN, 0) is KN [q <= 1] and maps NaN to 0
             const float lp   = lg2_normal(pq);
             const float poly = __fmaf_rn(__fmaf_rn(kC2, pq, B1[k]), pq, A0[k]);
             const float kn   = __fmaf_rn(pq, lp, poly);
-            acc[k]           = __fmaf_rn(w, pq <= kL ? kn : 0.0f, acc[k]);
+            acc[k]           = __fmaf_rn(w, fmaxf(kn, 0.0f), acc[k]);
           }
         }
         // scale by e^2 f_g / g^k and fold into the double-float sums

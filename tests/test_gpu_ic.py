@@ -64,6 +64,30 @@ def test_invalid_and_unreachable_bins(gpu, oracle_lib):
     assert max_rel(got[good], want) <= SPECTRUM_RTOL
 
 
+def test_wide_and_masked_soft_photons(gpu, oracle_lib):
+    """Soft photons over 39 decades in one 64-photon chunk (q from far below 1e-30 to far
+    above 1: the floor on t/g and max(KN, 0) at both ends), a ragged last chunk, and masked
+    photons (e_s <= 0, NaN, 1/(4 e_s) overflowing) that contribute nothing."""
+    gb = oracle_lib.logspace(10.0, 1e6, 200)
+    fp = (gb.astype(np.float64) ** -2.0).astype(np.float32)
+    es = np.concatenate([oracle_lib.logspace(1e-36, 1e3, 64),
+                         oracle_lib.logspace(1e-9, 1e-5, 64),
+                         oracle_lib.logspace(1e-9, 1e-5, 40)])
+    fs = np.ones(len(es), np.float32)
+    eic = oracle_lib.logspace(1e-3, 1e6, 300)
+    got = gpu_ic(gb, fp, True, es, fs, eic, gpu)
+    assert max_rel(got, oracle_lib.ic_spectrum_f64(gb, fp, True, es, fs, eic)) <= SPECTRUM_RTOL
+
+    bad = es.copy()
+    idx = [3, 70, 130, 150]
+    bad[idx] = [0.0, -1e-8, np.nan, 1e-45]  # the last: 4 e_s is subnormal, 1/(4 e_s) = inf
+    keep = np.ones(len(es), bool)
+    keep[idx] = False
+    got = gpu_ic(gb, fp, True, bad, fs, eic, gpu)
+    want = oracle_lib.ic_spectrum_f64(gb, fp, True, bad[keep], fs[keep], eic)
+    assert max_rel(got, want) <= SPECTRUM_RTOL
+
+
 def test_empty_inputs(gpu):
     dev = gpu
     z = torch.zeros(4, device=dev)
