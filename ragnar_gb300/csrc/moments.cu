@@ -110,7 +110,15 @@ namespace rg {
       const int64_t  first  = m.seg_off ? soff[0] : 0;
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
       const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-      for (int64_t i = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < last; i += stride) {
+      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      // this thread's segment, advanced as its particle index grows
+      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
+      for (int64_t i = i0; i < last; i += stride) {
+        if (m.seg_off) {
+          while (seg < m.nseg && soff[seg + 1] <= i) {
+            ++seg;
+          }
+        }
         float v[kComps];
 #pragma unroll
         for (int c = 0; c < kComps; ++c) {
@@ -136,10 +144,6 @@ namespace rg {
           } else {
             hi = mid;
           }
-        }
-        int seg = 0;
-        if (m.seg_off) {
-          seg = segment_of(soff, m.nseg, i);
         }
         if (Rc >= static_cast<uint32_t>(nc) || seg >= m.nseg) { // self-check: never taken for live particles
           atomicOr(m.fp.status, kDevBadIndex);

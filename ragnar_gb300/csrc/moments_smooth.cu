@@ -96,7 +96,15 @@ namespace rg {
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
       const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
       const uint32_t mask   = (1u << m.F) - 1u;
-      for (int64_t i = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < last; i += stride) {
+      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      // this thread's segment, advanced as its particle index grows
+      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
+      for (int64_t i = i0; i < last; i += stride) {
+        if (m.seg_off) {
+          while (seg < m.nseg && soff[seg + 1] <= i) {
+            ++seg;
+          }
+        }
         float v[kComps];
 #pragma unroll
         for (int c = 0; c < kComps; ++c) {
@@ -111,7 +119,6 @@ namespace rg {
         const uint32_t Rc  = static_cast<uint32_t>(R >> m.F);
         const uint32_t Rl  = static_cast<uint32_t>(R) & mask;
         const int      sub = static_cast<int>(((Rl >> (m.F - kSubBits)) + threadIdx.x) & (kSub - 1));
-        const int      seg = m.seg_off ? segment_of(soff, m.nseg, i) : 0;
         if (Rc >= static_cast<uint32_t>(m.nc) || seg >= m.nseg) { // self-check: never taken for live particles
           atomicOr(m.fp.status, kDevBadIndex);
           continue;
@@ -312,7 +319,15 @@ namespace rg {
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
       const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
       const uint32_t mask   = (1u << m.F) - 1u;
-      for (int64_t i = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < last; i += stride) {
+      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      // this thread's segment, advanced as its particle index grows
+      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
+      for (int64_t i = i0; i < last; i += stride) {
+        if (m.seg_off) {
+          while (seg < m.nseg && soff[seg + 1] <= i) {
+            ++seg;
+          }
+        }
         float v[kComps];
 #pragma unroll
         for (int c = 0; c < kComps; ++c) {
@@ -325,7 +340,6 @@ namespace rg {
           const uint64_t R   = static_cast<uint64_t>(m.Pmax - Q);
           const uint32_t Rc  = static_cast<uint32_t>(R >> m.F);
           const uint32_t Rl  = static_cast<uint32_t>(R) & mask;
-          const int      seg = m.seg_off ? segment_of(soff, m.nseg, i) : 0;
           if (Rc < static_cast<uint32_t>(m.nc) && seg < m.nseg) {
             const float  tau = __uint2float_rn(Rl) * m.tau_scale;
             const float4 al  = __ldg(a.alpha + static_cast<int64_t>(seg) * m.nc + Rc);
