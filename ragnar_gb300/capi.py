@@ -155,8 +155,11 @@ def addr(t) -> int:
 
 
 def particles(u, b=None, e=None, w=None, n=None) -> Particles:
-    """Build an rg_particles from 3-sequences of device tensors (or None)."""
+    """Build an rg_particles from 3-sequences of device tensors (or None).  The returned
+    structure holds references to the tensors, so that temporaries passed here stay
+    allocated while the structure is in use."""
     p = Particles()
+    p._refs = (u, b, e, w)
     for d in range(3):
         p.u[d] = addr(u[d])
         p.e[d] = addr(e[d]) if e is not None else 0
@@ -167,7 +170,8 @@ def particles(u, b=None, e=None, w=None, n=None) -> Particles:
 
 
 def host_particles(u, b=None, e=None, w=None, n=None) -> Particles:
-    """rg_particles over HOST arrays (numpy arrays or pinned CPU tensors)."""
+    """rg_particles over HOST arrays (numpy arrays or pinned CPU tensors); holds references
+    to the arrays like particles()."""
 
     def hp(a):
         if a is None:
@@ -177,6 +181,7 @@ def host_particles(u, b=None, e=None, w=None, n=None) -> Particles:
         return int(a.ctypes.data)
 
     p = Particles()
+    p._refs = (u, b, e, w)
     for d in range(3):
         p.u[d] = hp(u[d])
         p.e[d] = hp(e[d]) if e is not None else 0

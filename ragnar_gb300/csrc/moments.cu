@@ -473,9 +473,12 @@ namespace rg {
     cudaFree(pl->d_binfo);
     cudaFree(pl->d_mcoef);
     cudaFree(pl->d_hist);
-    cudaFree(pl->d_alpha);
+    cudaFree(pl->d_cells);
+    cudaFree(pl->d_coef64);
     cudaFree(pl->own_smooth.d_coef);
-    pl->d_alpha           = nullptr;
+    pl->d_cells           = nullptr;
+    pl->cells_cap         = 0;
+    pl->d_coef64          = nullptr;
     pl->own_smooth.d_coef = nullptr;
     pl->d_mslice = nullptr;
     pl->d_mrange = nullptr;

@@ -41,13 +41,11 @@ namespace rg {
     // Slots per cell: a particle adds its moments (which are absolute within the cell) to
     // the slot of its lane, shifted by its position in the cell, so the lanes of a warp
     // whose particles crowd one cell hit different addresses.
-    constexpr int    kSub         = 32;
-    constexpr int    kSubBits     = 5;
+    constexpr int    kSub         = 64;
+    constexpr int    kSubBits     = 6;
     constexpr int    kSmThreads   = 256;
     constexpr int    kSmSharedSeg = 1024;      // segment offsets staged in shared memory
-    constexpr int    kSmRows      = 16;        // segment groups of the reduce kernel
     constexpr double kTargetDln   = 0.0089954; // ln(1e8) / 2048: the device-wide table's spacing
-    constexpr size_t kSmSharedMax = 200 * 1024; // shared-memory cell table of the block-aggregated deposit
     // Largest bin residual |eps_b|, in table segments.  Logbins-style bins carry ~2e-6 in
     // ln e (their exponent is rounded to float before the power); the first-order
     // correction leaves eps^2 |F''| / 2 < 1e-6 F at this bound.
@@ -133,79 +131,40 @@ namespace rg {
       }
     }
 
-    // Single-segment runs whose cell table fits in shared memory: one 1024-thread block per
-    // SM accumulates the four moments of every cell in shared memory (FP64 atomics on the
-    // block's own copy) and adds its copy to slot 0 of the global table once at the end, so
-    // the global atomics are per (block, cell), not per particle.
-    constexpr int kSmSharedThreads = 1024;
-
-    __global__ void __launch_bounds__(kSmSharedThreads, 1)
-      smooth_deposit_shared_kernel(const __grid_constant__ SmoothMomParams m) {
-      extern __shared__ __align__(16) double cellm[]; // nc x 4
-      for (int i = threadIdx.x; i < m.nc * 4; i += blockDim.x) {
-        cellm[i] = 0.0;
-      }
-      if (__syncthreads_or(*m.fp.status != kDevOk)) {
-        return;
-      }
-      const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-      const uint32_t mask   = (1u << m.F) - 1u;
-      for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-        float v[kComps];
-#pragma unroll
-        for (int c = 0; c < kComps; ++c) {
-          v[c] = m.fp.comp[c] ? __ldg(m.fp.comp[c] + i) : 0.0f;
-        }
-        int64_t Q = 0;
-        float   A = 0.0f;
-        if (!moment_particle_stage(v, m.fp, m.Pmin, m.Pmax, m.L, Q, A)) {
-          continue;
-        }
-        const uint64_t R  = static_cast<uint64_t>(m.Pmax - Q);
-        const uint32_t Rc = static_cast<uint32_t>(R >> m.F);
-        if (Rc >= static_cast<uint32_t>(m.nc)) { // self-check: never taken for live particles
-          atomicOr(m.fp.status, kDevBadIndex);
-          continue;
-        }
-        const float tau = __uint2float_rn(static_cast<uint32_t>(R) & mask) * m.tau_scale;
-        const float a1  = A * tau, a2 = a1 * tau, a3 = a2 * tau;
-        double*     h   = cellm + Rc * 4;
-        atomicAdd(h + 0, static_cast<double>(A));
-        atomicAdd(h + 1, static_cast<double>(a1));
-        atomicAdd(h + 2, static_cast<double>(a2));
-        atomicAdd(h + 3, static_cast<double>(a3));
-      }
-      __syncthreads();
-      for (int i = threadIdx.x; i < m.nc * 4; i += blockDim.x) {
-        const double x = cellm[i];
-        if (x != 0.0) {
-          atomicAdd(m.hist + (static_cast<int64_t>(i >> 2) * kSub) * 4 + (i & 3), x);
-        }
-      }
-    }
-
-    // Sums each cell's sub-cells into sub-cell 0 (thread per (segment, cell, moment)).
-    __global__ void smooth_fold_kernel(double* hist, int64_t cells_total) {
+    // Sums each cell's sub-cells into the compact cell table cells[seg][cell][4] (thread per
+    // (segment, cell, moment)).
+    __global__ void smooth_fold_kernel(const double* __restrict__ hist, int64_t cells_total, double* __restrict__ cells) {
       const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
       if (t >= cells_total * 4) {
         return;
       }
-      const int64_t cell = t >> 2;
-      const int     j    = static_cast<int>(t & 3);
-      double*       h    = hist + cell * kSub * 4 + j;
-      double        s    = 0.0;
+      const double* h = hist + (t >> 2) * kSub * 4 + (t & 3);
+      double        s = 0.0;
 #pragma unroll
       for (int k = 0; k < kSub; ++k) {
         s += h[k * 4];
       }
-      h[0] = s;
+      cells[t] = s;
+    }
+
+    // The table's coefficients as doubles for the reduce: (c0, c1), (c2, c3), and the
+    // coefficients of the first-order bin-residual term (c1, 2 c2), (3 c3, 0).
+    __global__ void smooth_coef64_kernel(const float4* __restrict__ coef, int nseg, double2* __restrict__ out) {
+      const int s = blockIdx.x * blockDim.x + threadIdx.x;
+      if (s < nseg) {
+        const float4 k = coef[s];
+        out[4 * s + 0] = make_double2(k.x, k.y);
+        out[4 * s + 1] = make_double2(k.z, k.w);
+        out[4 * s + 2] = make_double2(k.y, 2.0 * static_cast<double>(k.z));
+        out[4 * s + 3] = make_double2(3.0 * static_cast<double>(k.w), 0.0);
+      }
     }
 
     struct SmoothReduceParams {
-      const double*   hist; // folded: cell moments at sub-cell 0
+      const double*   cells;  // nseg x nc x 4 folded cell moments
       int             nc;
-      const int4*     binfo; // per bin: (Dc, eps bits, 0, valid)
-      const float4*   coef;  // the plan's table, nseg segments
+      const int4*     binfo;  // per bin: (Dc, eps bits, 0, valid)
+      const double2*  coef64; // per table segment: 4 double2 (smooth_coef64_kernel)
       int             nseg_tab;
       int             nbins;
       const float*    ebins;
@@ -213,51 +172,63 @@ namespace rg {
       float*          out; // nseg x nbins
     };
 
-    __global__ void __launch_bounds__(32 * kSmRows) smooth_reduce_kernel(const __grid_constant__ SmoothReduceParams r) {
-      __shared__ double part[kSmRows][33];
-      const int  bin    = blockIdx.x * 32 + threadIdx.x;
+    // S_b / e_b = sum_s sum_j c'_j(s) M_j(Dc_b + s) = A + eps_b B with A = sum c_j M_j and
+    // B = sum (j + 1) c_{j+1} M_j: one 256-thread block per (bin, segment), its threads taking
+    // every 256th table segment (consecutive cells: coalesced), FP64, summed in a fixed order.
+    constexpr int kSmRedThreads = 256;
+
+    __global__ void __launch_bounds__(kSmRedThreads) smooth_reduce_kernel(const __grid_constant__ SmoothReduceParams r) {
+      __shared__ double wsum[kSmRedThreads / 32];
+      const int  bin    = blockIdx.x;
       const int  seg    = blockIdx.y;
       const bool failed = *r.status != kDevOk;
-      int4       bi     = make_int4(0, 0, 0, 0);
-      if (bin < r.nbins && !failed) {
-        bi = r.binfo[bin];
-      }
-      double sum = 0.0;
-      if (bi.w) {
-        const double  eps = static_cast<double>(__int_as_float(bi.y));
-        const double* h   = r.hist + static_cast<int64_t>(seg) * r.nc * kSub * 4;
-        for (int s = threadIdx.y; s < r.nseg_tab; s += kSmRows) {
-          const int c = bi.x + s;
-          if (c >= r.nc) {
-            break;
-          }
-          const float4  k  = __ldg(r.coef + s);
-          const double* M  = h + static_cast<int64_t>(c) * kSub * 4;
-          const double  c0 = k.x, c1 = k.y, c2 = k.z, c3 = k.w;
-          sum += (c0 + eps * c1) * M[0] + (c1 + 2.0 * eps * c2) * M[1] + (c2 + 3.0 * eps * c3) * M[2] + c3 * M[3];
+      const int4 bi     = r.binfo[bin];
+      double     t      = 0.0;
+      if (bi.w && !failed) {
+        const double2* M    = reinterpret_cast<const double2*>(r.cells + (static_cast<int64_t>(seg) * r.nc + bi.x) * 4);
+        const int      smax = min(r.nseg_tab, r.nc - bi.x);
+        double         a = 0.0, b = 0.0;
+        for (int s = threadIdx.x; s < smax; s += kSmRedThreads) {
+          const double2 m01 = M[2 * s], m23 = M[2 * s + 1];
+          const double2 c01 = __ldg(r.coef64 + 4 * s), c23 = __ldg(r.coef64 + 4 * s + 1);
+          const double2 d01 = __ldg(r.coef64 + 4 * s + 2), d23 = __ldg(r.coef64 + 4 * s + 3);
+          a = fma(c01.x, m01.x, a);
+          a = fma(c01.y, m01.y, a);
+          a = fma(c23.x, m23.x, a);
+          a = fma(c23.y, m23.y, a);
+          b = fma(d01.x, m01.x, b);
+          b = fma(d01.y, m01.y, b);
+          b = fma(d23.x, m23.x, b);
         }
+        t = fma(static_cast<double>(__int_as_float(bi.y)), b, a);
       }
-      part[threadIdx.y][threadIdx.x] = sum;
-      __syncthreads();
-      if (threadIdx.y != 0 || bin >= r.nbins) {
-        return;
-      }
-      double result = 0.0;
-      if (failed) {
-        result = __longlong_as_double(0x7ff8000000000000LL);
-      } else if (bi.w) {
-        double t = 0.0;
 #pragma unroll
-        for (int y = 0; y < kSmRows; ++y) {
-          t += part[y][threadIdx.x];
-        }
-        result = t * static_cast<double>(r.ebins[bin]);
+      for (int o = 16; o > 0; o >>= 1) {
+        t += __shfl_down_sync(0xffffffffu, t, o);
       }
-      r.out[static_cast<int64_t>(seg) * r.nbins + bin] = __double2float_rn(result);
+      if ((threadIdx.x & 31) == 0) {
+        wsum[threadIdx.x >> 5] = t;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double result = 0.0;
+        if (failed) {
+          result = __longlong_as_double(0x7ff8000000000000LL);
+        } else if (bi.w) {
+          double u = 0.0;
+#pragma unroll
+          for (int w = 0; w < kSmRedThreads / 32; ++w) {
+            u += wsum[w];
+          }
+          result = u * static_cast<double>(r.ebins[bin]);
+        }
+        r.out[static_cast<int64_t>(seg) * r.nbins + bin] = __double2float_rn(result);
+      }
     }
 
-    // alpha_j(c) = sum_b G_b e_b c'_j(c - Dc_b) for every (segment, cell): FP32 products,
-    // compensated (Kahan) sums.  Thread per (segment, cell).
+    // alpha_j(c) = sum_b G_b e_b c'_j(c - Dc_b) for every (segment, cell): one warp per
+    // (segment, cell), its lanes taking every 32nd bin with FP32 products and compensated
+    // (Kahan) sums, then a double-float sum over the lanes in a fixed order.
     struct SmoothAlphaParams {
       const float*  grad_out; // nseg x nbins
       const int4*   binfo;
@@ -277,14 +248,17 @@ namespace rg {
       s             = t;
     }
 
-    __global__ void smooth_alpha_kernel(const __grid_constant__ SmoothAlphaParams a) {
-      const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (t >= static_cast<int64_t>(a.nseg) * a.nc) {
+    constexpr int kSmAlphaThreads = 256;
+
+    __global__ void __launch_bounds__(kSmAlphaThreads) smooth_alpha_kernel(const __grid_constant__ SmoothAlphaParams a) {
+      const int64_t t    = (static_cast<int64_t>(blockIdx.x) * kSmAlphaThreads + threadIdx.x) >> 5;
+      const int     lane = threadIdx.x & 31;
+      if (t >= static_cast<int64_t>(a.nseg) * a.nc) { // warp-uniform
         return;
       }
       const int seg = static_cast<int>(t / a.nc), c = static_cast<int>(t % a.nc);
       float     s[4] = { 0.f, 0.f, 0.f, 0.f }, e[4] = { 0.f, 0.f, 0.f, 0.f };
-      for (int b = 0; b < a.nbins; ++b) {
+      for (int b = lane; b < a.nbins; b += 32) {
         const int4 bi = __ldg(a.binfo + b);
         const int  sg = c - bi.x;
         if (!bi.w || sg < 0 || sg >= a.nseg_tab) {
@@ -298,7 +272,26 @@ namespace rg {
         kahan_add(s[2], e[2], g * fmaf(3.0f * eps, k.w, k.z));
         kahan_add(s[3], e[3], g * k.w);
       }
-      a.alpha[t] = make_float4(s[0], s[1], s[2], s[3]);
+      float out[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        // the lane's sum is s - e; add the lanes' double-floats pairwise
+        ff v = fast_two_sum(s[j], -e[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float oh = __shfl_xor_sync(0xffffffffu, v.hi, o);
+          const float ol = __shfl_xor_sync(0xffffffffu, v.lo, o);
+          // every lane forms the same sum in the same order: the lower lane's value first
+          const bool lower = (lane & o) == 0;
+          const ff   x = lower ? v : ff { oh, ol }, y = lower ? ff { oh, ol } : v;
+          const ff   h = two_sum(x.hi, y.hi);
+          v          = fast_two_sum(h.hi, __fadd_rn(h.lo, __fadd_rn(x.lo, y.lo)));
+        }
+        out[j] = __fadd_rn(v.hi, v.lo);
+      }
+      if (lane == 0) {
+        a.alpha[t] = make_float4(out[0], out[1], out[2], out[3]);
+      }
     }
 
     struct SmoothAdjParams {
@@ -466,7 +459,23 @@ namespace rg {
     pl->hist_per_seg = cells * kSub * 2; // double2 entries: kSub x 4 doubles per cell
     RG_CUDA_TRY(cudaMalloc(&pl->d_binfo, sizeof(int4) * binfo.size()));
     RG_CUDA_TRY(cudaMemcpy(pl->d_binfo, binfo.data(), sizeof(int4) * binfo.size(), cudaMemcpyHostToDevice));
+    RG_CUDA_TRY(cudaMalloc(&pl->d_coef64, sizeof(double2) * 4 * static_cast<size_t>(t->nseg)));
+    smooth_coef64_kernel<<<(t->nseg + 127) / 128, 128>>>(t->d_coef, t->nseg, pl->d_coef64);
+    RG_CUDA_TRY(cudaGetLastError());
+    RG_CUDA_TRY(cudaDeviceSynchronize());
     pl->moments_ok = true;
+    return RG_OK;
+  }
+
+  // Per-(segment, cell) scratch for at least `entries` (segment, cell) pairs.
+  int smooth_reserve_cells(rg_spectrum_plan* pl, size_t entries) {
+    if (entries > pl->cells_cap) {
+      cudaFree(pl->d_cells);
+      pl->d_cells   = nullptr;
+      pl->cells_cap = 0;
+      RG_CUDA_TRY(cudaMalloc(&pl->d_cells, sizeof(double) * 4 * entries));
+      pl->cells_cap = entries;
+    }
     return RG_OK;
   }
 
@@ -490,18 +499,7 @@ namespace rg {
       }
       RG_CUDA_TRY(cudaEventRecord(ev.first, s));
     }
-    const size_t cell_bytes = sizeof(double) * 4 * static_cast<size_t>(pl->sm_cells);
-    if (!d_off && cell_bytes <= kSmSharedMax) {
-      static std::atomic<uint64_t> configured { 0 };
-      RG_CUDA_TRY(ensure_max_dynamic_smem(smooth_deposit_shared_kernel, static_cast<int>(kSmSharedMax), configured));
-      DeviceContext* ctx = nullptr;
-      RG_TRY(context(&ctx));
-      const int64_t need = (n + kSmSharedThreads - 1) / kSmSharedThreads;
-      const int     g1   = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, ctx->sms)));
-      smooth_deposit_shared_kernel<<<g1, kSmSharedThreads, cell_bytes, s>>>(m);
-    } else {
-      smooth_deposit_kernel<<<grid, kSmThreads, 0, s>>>(m);
-    }
+    smooth_deposit_kernel<<<grid, kSmThreads, 0, s>>>(m);
     RG_CUDA_TRY(cudaGetLastError());
     if (pl->timing) {
       RG_CUDA_TRY(cudaEventRecord(ev.second, s));
@@ -512,20 +510,21 @@ namespace rg {
 
   int smooth_moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s) {
     const int64_t cells_total = static_cast<int64_t>(nseg) * pl->sm_cells;
+    RG_TRY(smooth_reserve_cells(pl, static_cast<size_t>(cells_total)));
     smooth_fold_kernel<<<static_cast<int>((cells_total * 4 + 255) / 256), 256, 0, s>>>(
-      reinterpret_cast<double*>(pl->d_hist), cells_total);
+      reinterpret_cast<const double*>(pl->d_hist), cells_total, pl->d_cells);
     RG_CUDA_TRY(cudaGetLastError());
     SmoothReduceParams r {};
-    r.hist     = reinterpret_cast<const double*>(pl->d_hist);
+    r.cells    = pl->d_cells;
     r.nc       = pl->sm_cells;
     r.binfo    = pl->d_binfo;
-    r.coef     = pl->smooth->d_coef;
+    r.coef64   = pl->d_coef64;
     r.nseg_tab = pl->smooth->nseg;
     r.nbins    = pl->nbins;
     r.ebins    = pl->d_ebins;
     r.status   = pl->d_status;
     r.out      = out;
-    smooth_reduce_kernel<<<dim3((pl->nbins + 31) / 32, nseg), dim3(32, kSmRows), 0, s>>>(r);
+    smooth_reduce_kernel<<<dim3(pl->nbins, nseg), kSmRedThreads, 0, s>>>(r);
     RG_CUDA_TRY(cudaGetLastError());
     return RG_OK;
   }
@@ -536,12 +535,7 @@ namespace rg {
                              int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s) {
     const int    nsg  = d_off ? nseg : 1;
     const size_t need = static_cast<size_t>(nsg) * pl->sm_cells;
-    if (need > pl->alpha_cap) {
-      cudaFree(pl->d_alpha);
-      pl->d_alpha = nullptr;
-      RG_CUDA_TRY(cudaMalloc(&pl->d_alpha, sizeof(float4) * need));
-      pl->alpha_cap = need;
-    }
+    RG_TRY(smooth_reserve_cells(pl, need));
     SmoothAlphaParams a {};
     a.grad_out = grad_out;
     a.binfo    = pl->d_binfo;
@@ -551,15 +545,15 @@ namespace rg {
     a.ebins    = pl->d_ebins;
     a.nc       = pl->sm_cells;
     a.nseg     = nsg;
-    a.alpha    = pl->d_alpha;
-    smooth_alpha_kernel<<<static_cast<int>((need + 127) / 128), 128, 0, s>>>(a);
+    a.alpha    = reinterpret_cast<float4*>(pl->d_cells);
+    smooth_alpha_kernel<<<static_cast<int>((need * 32 + kSmAlphaThreads - 1) / kSmAlphaThreads), kSmAlphaThreads, 0, s>>>(a);
     RG_CUDA_TRY(cudaGetLastError());
     if (n == 0 && !d_off) {
       return RG_OK;
     }
     SmoothAdjParams x {};
     fill_smooth_params(pl, comp, d_off, n, nseg, x.m);
-    x.alpha   = pl->d_alpha;
+    x.alpha   = reinterpret_cast<const float4*>(pl->d_cells);
     x.inv_dln = static_cast<float>(1.0 / pl->smooth->dln);
     x.gw      = gw;
     for (int d = 0; d < 3; ++d) {

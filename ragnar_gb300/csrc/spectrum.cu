@@ -742,13 +742,9 @@ namespace rg {
         RG_CUDA_TRY(cudaMalloc(&pl->d_hist, sizeof(double2) * need));
         pl->hist_cap = need;
       }
-      // the moment adjoint's per-cell cubics
-      const size_t alpha = pl->aligned ? static_cast<size_t>(max_seg) * pl->sm_cells : 0;
-      if (alpha > pl->alpha_cap) {
-        cudaFree(pl->d_alpha);
-        pl->d_alpha = nullptr;
-        RG_CUDA_TRY(cudaMalloc(&pl->d_alpha, sizeof(float4) * alpha));
-        pl->alpha_cap = alpha;
+      // the smooth moment path's per-cell scratch (folded moments, adjoint cubics)
+      if (pl->aligned) {
+        RG_TRY(smooth_reserve_cells(pl, static_cast<size_t>(max_seg) * pl->sm_cells));
       }
     }
     return RG_OK;

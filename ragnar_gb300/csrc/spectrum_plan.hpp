@@ -58,8 +58,10 @@ struct rg_spectrum_plan {
   bool                  aligned     = false;
   int64_t               sm_pmin = 0, sm_pmax = 0; // smallest / largest bin coordinate, fine units
   int                   sm_cells    = 0;
-  float4*               d_alpha     = nullptr; // adjoint cell cubics, nseg x cells
-  size_t                alpha_cap   = 0;
+  double*               d_cells     = nullptr; // nseg x cells x 4 doubles: the forward's folded cell
+                                               // moments, or (as float4) the adjoint's cell cubics
+  size_t                cells_cap   = 0;       // (segment, cell) entries
+  double2*              d_coef64    = nullptr; // per table segment: (c0, c1), (c2, c3), (c1, 2 c2), (3 c3, 0)
   // kernel timing (events bracketing each fused launch)
   bool                                             timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_free;
@@ -92,6 +94,7 @@ namespace rg {
   // The smooth-table variant (moments_smooth.cu).
   int  smooth_align_plan(rg_spectrum_plan* pl, double ln_k0);
   int  smooth_moments_prepare(rg_spectrum_plan* pl, double ln_k0);
+  int  smooth_reserve_cells(rg_spectrum_plan* pl, size_t entries);
   int  smooth_moments_deposit(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
                               int nseg, cudaStream_t s);
   int  smooth_moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s);

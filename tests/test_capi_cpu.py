@@ -136,3 +136,29 @@ def test_module_exposes_reference_api():
     assert rg.EnergyUnits.mec2 == "mec2" and rg.EnergyUnits.mpc2 == "mpc2"
     p = rg.Particles_3D("electrons")
     assert p.label() == "electrons" and not p.is_allocated() and len(p) == 0
+
+
+def test_particle_structs_keep_their_arrays():
+    """rg_particles holds raw addresses: the Python structure keeps the arrays it was built
+    from alive, so temporaries passed to particles() / host_particles() are not freed (and
+    their memory reused by later allocations) while the structure is in use."""
+    import gc  # noqa: PLC0415
+    import weakref  # noqa: PLC0415
+
+    torch = pytest.importorskip("torch")
+    t = torch.ones(8)
+    ref = weakref.ref(t)
+    p = capi.particles([t, t, t], b=[None, None, torch.zeros(8)])
+    del t
+    gc.collect()
+    assert ref() is not None and p.u[0] == ref().data_ptr()
+    del p
+    gc.collect()
+    assert ref() is None
+
+    a = np.ones(8, np.float32)
+    ref = weakref.ref(a)
+    h = capi.host_particles([a, a, a])
+    del a
+    gc.collect()
+    assert ref() is not None and h.u[0] == ref().ctypes.data
