@@ -53,8 +53,7 @@ namespace rg {
     constexpr int kMomBucketBits = kMomFrac - 12;
     constexpr int kMomSharedSeg  = 1024;             // segment offsets staged in shared memory
     constexpr int kMomThreads    = 256;
-    constexpr int kMomRows       = 16;               // cell groups of the reduce kernel
-    constexpr int kMomMaxTable   = 256;              // table segments the reduce kernel stages
+    constexpr int kMomMaxTable   = 256;              // largest reference table (segments) this path takes
     constexpr size_t kMomMaxBytes = size_t(8) << 30; // histogram memory above which the fused kernel runs
 
     struct MomentParams {
@@ -161,7 +160,11 @@ namespace rg {
     }
 
     // In-place inclusive prefix sums along each cell's row of interval moments: one warp
-    // per row (cell), rows of (segment, slice) blockIdx.y.
+    // per row (cell), rows of (segment, slice) blockIdx.y.  Each lane takes a contiguous
+    // chunk of the row (its loads independent, all in flight at once), sums it, and adds
+    // the exclusive warp scan of the chunk totals.
+    constexpr int kScanChunk = (kSliceBins + 1 + 31) / 32; // entries per lane for the longest row
+
     __global__ void __launch_bounds__(256) moments_scan_kernel(double2* hist, const int4* mslice, int nslices,
                                                                int64_t per_seg) {
       const int  seg = blockIdx.y / nslices, slice = blockIdx.y % nslices;
@@ -172,27 +175,41 @@ namespace rg {
         return;
       }
       const int row = ms.x + 1;
+      const int C   = (row + 31) >> 5;
+      const int j0  = lane * C;
       double2*  r   = hist + seg * per_seg + ms.z + static_cast<int64_t>(cell) * row;
-      double    c0 = 0.0, c1 = 0.0;
-      for (int j0 = 0; j0 < row; j0 += 32) {
-        const int j = j0 + lane;
-        double2   v = j < row ? r[j] : make_double2(0.0, 0.0);
+      double2   v[kScanChunk];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const double a = __shfl_up_sync(0xffffffffu, v.x, o);
-          const double b = __shfl_up_sync(0xffffffffu, v.y, o);
-          if (lane >= o) {
-            v.x += a;
-            v.y += b;
-          }
+      for (int k = 0; k < kScanChunk; ++k) {
+        v[k] = (k < C && j0 + k < row) ? r[j0 + k] : make_double2(0.0, 0.0);
+      }
+      double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+      for (int k = 0; k < kScanChunk; ++k) {
+        s0 += v[k].x;
+        s1 += v[k].y;
+        v[k] = make_double2(s0, s1);
+      }
+      // inclusive scan of the chunk totals, shifted by one lane: the exclusive offsets
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double a = __shfl_up_sync(0xffffffffu, s0, o);
+        const double b = __shfl_up_sync(0xffffffffu, s1, o);
+        if (lane >= o) {
+          s0 += a;
+          s1 += b;
         }
-        v.x += c0;
-        v.y += c1;
-        if (j < row) {
-          r[j] = v;
+      }
+      double e0 = __shfl_up_sync(0xffffffffu, s0, 1), e1 = __shfl_up_sync(0xffffffffu, s1, 1);
+      if (lane == 0) {
+        e0 = 0.0;
+        e1 = 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kScanChunk; ++k) {
+        if (k < C && j0 + k < row) {
+          r[j0 + k] = make_double2(v[k].x + e0, v[k].y + e1);
         }
-        c0 = __shfl_sync(0xffffffffu, v.x, 31);
-        c1 = __shfl_sync(0xffffffffu, v.y, 31);
       }
     }
 
@@ -209,48 +226,48 @@ namespace rg {
       float*          out;      // nseg x nbins
     };
 
-    // Block (32 bins x kMomRows cell groups) of one segment: each thread sums every
-    // kMomRows-th cell its bin's segments reach, then the groups combine in order.
-    __global__ void __launch_bounds__(32 * kMomRows) moments_reduce_kernel(const __grid_constant__ MomentReduceParams r) {
-      __shared__ double2 coef[kMomMaxTable];
-      __shared__ double  part[kMomRows][33];
-      const int tid = threadIdx.y * 32 + threadIdx.x;
-      for (int i = tid; i < r.nseg_tab; i += 32 * kMomRows) {
-        coef[i] = r.coef[i];
-      }
-      __syncthreads();
-      const int  bin    = blockIdx.x * 32 + threadIdx.x;
+    // One 256-thread block per (bin, segment): each thread takes every 256th cell the bin's
+    // table segments reach (at most nseg_tab + 1 cells), then the block sums in a fixed order.
+    constexpr int kMomRedThreads = 256;
+
+    __global__ void __launch_bounds__(kMomRedThreads) moments_reduce_kernel(const __grid_constant__ MomentReduceParams r) {
+      __shared__ double wsum[kMomRedThreads / 32];
+      const int  bin    = blockIdx.x;
       const int  seg    = blockIdx.y;
       const bool failed = *r.status != kDevOk;
+      const int4 bi     = r.binfo[bin];
       double     sum    = 0.0;
-      int4       bi     = make_int4(0, 0, 0, 0);
-      if (bin < r.nbins && !failed) {
-        bi = r.binfo[bin];
-      }
-      if (bi.w) {
-        const int      slice = bin / kSliceBins;
-        const int4     ms    = r.mslice[slice];
-        const int      row   = ms.x + 1;
-        const double2* h     = r.hist + seg * r.per_seg + ms.z;
+      if (bi.w && !failed) {
+        const int4     ms  = r.mslice[bin / kSliceBins];
+        const int      row = ms.x + 1;
+        const double2* h   = r.hist + seg * r.per_seg + ms.z;
         const int      pos = bi.x, Dc = bi.y;
         const double   Dl = static_cast<double>(bi.z), Dlw = Dl - static_cast<double>(1u << kMomFrac);
         const int      c_end = min(ms.y, Dc + r.nseg_tab + 1);
-        for (int c = Dc + threadIdx.y; c < c_end; c += kMomRows) {
+        for (int c = Dc + threadIdx.x; c < c_end; c += kMomRedThreads) {
           const double2 Lm = h[static_cast<int64_t>(c) * row + pos];
           const double2 Tm = h[static_cast<int64_t>(c) * row + ms.x];
           const int     s  = c - Dc;
           if (s < r.nseg_tab) { // intervals at or above Dl: segment s
-            const double U0 = Tm.x - Lm.x, U1 = Tm.y - Lm.y;
-            sum += coef[s].x * U0 + coef[s].y * (U1 - Dl * U0);
+            const double2 k  = __ldg(r.coef + s);
+            const double  U0 = Tm.x - Lm.x, U1 = Tm.y - Lm.y;
+            sum += k.x * U0 + k.y * (U1 - Dl * U0);
           }
           if (s >= 1) { // intervals below Dl: segment s - 1, position Rl - Dl + 2^F
-            sum += coef[s - 1].x * Lm.x + coef[s - 1].y * (Lm.y - Dlw * Lm.x);
+            const double2 k = __ldg(r.coef + s - 1);
+            sum += k.x * Lm.x + k.y * (Lm.y - Dlw * Lm.x);
           }
         }
       }
-      part[threadIdx.y][threadIdx.x] = sum;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        wsum[threadIdx.x >> 5] = sum;
+      }
       __syncthreads();
-      if (threadIdx.y != 0 || bin >= r.nbins) {
+      if (threadIdx.x != 0) {
         return;
       }
       double result = 0.0;
@@ -259,8 +276,8 @@ namespace rg {
       } else if (bi.w) {
         double t = 0.0;
 #pragma unroll
-        for (int y = 0; y < kMomRows; ++y) {
-          t += part[y][threadIdx.x];
+        for (int w = 0; w < kMomRedThreads / 32; ++w) {
+          t += wsum[w];
         }
         result = t * static_cast<double>(r.ebins[bin]);
       }
@@ -460,7 +477,7 @@ namespace rg {
     r.ebins    = pl->d_ebins;
     r.status   = pl->d_status;
     r.out      = out;
-    moments_reduce_kernel<<<dim3((pl->nbins + 31) / 32, nseg), dim3(32, kMomRows), 0, s>>>(r);
+    moments_reduce_kernel<<<dim3(pl->nbins, nseg), kMomRedThreads, 0, s>>>(r);
     RG_CUDA_TRY(cudaGetLastError());
     return RG_OK;
   }
