@@ -939,11 +939,29 @@ def fwd_adjoint_case(torch, capi, device):
             plan.adjoint(prt, gS, gw, gu, stream)
 
         t_step = timed(torch, step, 10)
-        plan.check(stream)
-        plan.close()
         res[name] = {"fwd_evals_per_s": evals / t_fwd, "adjoint_evals_per_s": evals / t_adj,
                      "fwd_plus_adjoint_evals_per_s": evals / t_step, "fwd_plus_adjoint_ms": t_step * 1e3,
                      "fwd_ms": t_fwd * 1e3, "adjoint_ms": t_adj * 1e3}
+        if plan.placement_supported():
+            # the pair as torch_ext runs it: the forward records each particle's placement
+            # (8 bytes per particle) and the adjoint reads it instead of placing the particle again
+            place = torch.empty(2 * n, device=device, dtype=torch.int32)
+
+            def step_placed():
+                plan.run_placed(prt, S, place, stream)
+                plan.adjoint_placed(prt, place, gS, gw, gu, stream)
+
+            t_fwd_p = timed(torch, lambda: plan.run_placed(prt, S, place, stream), 10)
+            t_adj_p = timed(torch, lambda: plan.adjoint_placed(prt, place, gS, gw, gu, stream), 10)
+            t_step_p = timed(torch, step_placed, 10)
+            res[name].update({
+                "unplaced_fwd_plus_adjoint_ms": t_step * 1e3, "fwd_plus_adjoint_ms": t_step_p * 1e3,
+                "fwd_plus_adjoint_evals_per_s": evals / t_step_p, "placed_fwd_ms": t_fwd_p * 1e3,
+                "placed_adjoint_ms": t_adj_p * 1e3,
+                "pair": "run_placed + adjoint_placed (the torch_ext path); fwd_ms / adjoint_ms: run + adjoint"})
+            del place
+        plan.check(stream)
+        plan.close()
     # moments: HBM roofline of the pair (forward reads 28 B per particle, the adjoint
     # reads 28 B and writes 16 B: dL/dw and dL/du)
     peak, src = measured_peak("hbm_gbs", 6800.0)

@@ -264,6 +264,22 @@ int rg_synchrotron_spectrum_noalloc(const rg_particles* p, const float* bins, in
 int rg_spectrum_adjoint(const rg_spectrum_plan* plan, const rg_particles* p, const float* grad_out,
                         float* grad_w, float* grad_ux, float* grad_uy, float* grad_uz, void* stream);
 
+/* Forward and adjoint with a placement record (extension): rg_spectrum_run_placed is
+ * rg_spectrum_run that also writes, for every particle of `p`, the table cell and the
+ * position inside it that place the particle on the plan's bin-aligned smooth table
+ * (`placement`: device memory of 8 bytes per particle, p->n entries); given that record,
+ * rg_spectrum_adjoint_placed skips the double-float particle stage that the adjoint
+ * otherwise repeats.  The adjoint's arguments must be the plan and particles of the forward
+ * that wrote the record (as for a tensor saved for a backward pass); results equal those of
+ * rg_spectrum_adjoint bit for bit.  Both need a plan that runs cell moments on its
+ * bin-aligned smooth table (RG_TABLE_SMOOTH over log-uniform bins, rg_spectrum_plan_algorithm
+ * reporting RG_ALGO_MOMENTS for one segment); otherwise RG_ERR_UNSUPPORTED. */
+int rg_spectrum_run_placed(rg_spectrum_plan* plan, const rg_particles* p, float* out, void* placement,
+                           void* stream);
+int rg_spectrum_adjoint_placed(rg_spectrum_plan* plan, const rg_particles* p, const void* placement,
+                               const float* grad_out, float* grad_w, float* grad_ux, float* grad_uy, float* grad_uz,
+                               void* stream);
+
 /* Batched adjoint: grad_out is [nseg x nbins], segments as rg_spectrum_run_batched. */
 int rg_spectrum_adjoint_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
                                 int32_t nseg, const float* grad_out, float* grad_w, float* grad_ux,

@@ -85,6 +85,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "rg_spectrum_run_batched": [_vp, ctypes.POINTER(Particles), _vp, _i32, _vp, _vp],
         "rg_spectrum_run_plain": [_vp, ctypes.POINTER(Particles), _vp, _vp],
         "rg_spectrum_run_host": [_vp, ctypes.POINTER(Particles), _vp, _vp],
+        "rg_spectrum_run_placed": [_vp, ctypes.POINTER(Particles), _vp, _vp, _vp],
+        "rg_spectrum_adjoint_placed": [_vp, ctypes.POINTER(Particles), _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "rg_spectrum_plan_enable_timing": [_vp, _i32],
         "rg_spectrum_plan_set_algorithm": [_vp, _i32],
         "rg_spectrum_plan_algorithm": [_vp, _i32, ctypes.POINTER(_i32)],
@@ -203,6 +205,7 @@ class SpectrumPlan:
         check(lib().rg_spectrum_plan_create(self.bins.ctypes.data, self.nbins, B0, g_syn, eps, mode,
                                             ctypes.byref(h)))
         self.handle = h
+        self.mode = mode
 
     def run(self, prt: Particles, out, stream: int = 0) -> None:
         check(lib().rg_spectrum_run(self.handle, ctypes.byref(prt), addr(out), stream))
@@ -254,6 +257,23 @@ class SpectrumPlan:
                 stream: int = 0) -> None:
         check(lib().rg_spectrum_adjoint(self.handle, ctypes.byref(prt), addr(grad_out), addr(grad_w),
                                         addr(grad_u[0]), addr(grad_u[1]), addr(grad_u[2]), stream))
+
+    def placement_supported(self) -> bool:
+        """Whether run_placed / adjoint_placed apply: cell moments on the plan's bin-aligned
+        smooth table for a single segment."""
+        return self.mode == RG_TABLE_SMOOTH and self.algorithm(1) == RG_ALGO_MOMENTS
+
+    def run_placed(self, prt: Particles, out, placement, stream: int = 0) -> None:
+        """run() that also writes each particle's table placement (8 bytes per particle) into
+        `placement` (a device buffer of at least prt.n * 8 bytes) for adjoint_placed."""
+        check(lib().rg_spectrum_run_placed(self.handle, ctypes.byref(prt), addr(out), addr(placement), stream))
+
+    def adjoint_placed(self, prt: Particles, placement, grad_out, grad_w=None, grad_u=(None, None, None),
+                       stream: int = 0) -> None:
+        """adjoint() from the placement a run_placed of the same particles wrote."""
+        check(lib().rg_spectrum_adjoint_placed(self.handle, ctypes.byref(prt), addr(placement), addr(grad_out),
+                                               addr(grad_w), addr(grad_u[0]), addr(grad_u[1]), addr(grad_u[2]),
+                                               stream))
 
     def adjoint_batched(self, prt: Particles, offsets, nseg: int, grad_out, grad_w=None,
                         grad_u=(None, None, None), stream: int = 0) -> None:

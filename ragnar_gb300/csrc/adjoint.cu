@@ -353,6 +353,25 @@ int rg_spectrum_adjoint(const rg_spectrum_plan* cplan, const rg_particles* p, co
                          static_cast<cudaStream_t>(stream));
 }
 
+int rg_spectrum_adjoint_placed(rg_spectrum_plan* plan, const rg_particles* p, const void* placement,
+                               const float* grad_out, float* grad_w, float* grad_ux, float* grad_uy, float* grad_uz,
+                               void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrumAdjoint");
+  if (!plan || !placement || !grad_out || plan->source != rg::kSrcParticles) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_adjoint_placed: bad arguments");
+  }
+  RG_TRY(rg::check_particles(p));
+  if (plan->zero || plan->nbins == 0 || !plan->aligned || !rg::moments_selected(plan, 1)) {
+    return rg::set_error(RG_ERR_UNSUPPORTED,
+                         "rg_spectrum_adjoint_placed: needs a plan that runs cell moments on its bin-aligned smooth table");
+  }
+  const float* comp[rg::kComps];
+  rg::particle_comps(p, comp);
+  float* gu[3] = { grad_ux, grad_uy, grad_uz };
+  return rg::smooth_moments_adjoint(plan, comp, nullptr, p->n, 1, grad_out, grad_w, gu,
+                                    static_cast<cudaStream_t>(stream), static_cast<const uint2*>(placement));
+}
+
 int rg_spectrum_adjoint_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
                                 int32_t nseg, const float* grad_out, float* grad_w, float* grad_ux,
                                 float* grad_uy, float* grad_uz, void* stream) {

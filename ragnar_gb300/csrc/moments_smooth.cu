@@ -61,7 +61,11 @@ namespace rg {
       int64_t        n;
       int            nc;        // cells
       double*        hist;      // [nseg][nc][kSub][4]
+      uint2*         place;     // single-segment runs: per particle (cell, fraction bits) or
+                                // (kNoCell, 0) for a particle that adds nothing; null: not kept
     };
+
+    constexpr uint32_t kNoCell = 0xffffffffu;
 
     // Stages and checks the segment offsets (as the interval-moment deposit does); false
     // for the whole block if they are bad or the status word is set.
@@ -111,6 +115,9 @@ namespace rg {
         int64_t Q = 0;
         float   A = 0.0f;
         if (!moment_particle_stage(v, m.fp, m.Pmin, m.Pmax, m.L, Q, A)) {
+          if (m.place) {
+            m.place[i] = make_uint2(kNoCell, 0u);
+          }
           continue;
         }
         const uint64_t R   = static_cast<uint64_t>(m.Pmax - Q);
@@ -119,7 +126,13 @@ namespace rg {
         const int      sub = static_cast<int>(((Rl >> (m.F - kSubBits)) + threadIdx.x) & (kSub - 1));
         if (Rc >= static_cast<uint32_t>(m.nc) || seg >= m.nseg) { // self-check: never taken for live particles
           atomicOr(m.fp.status, kDevBadIndex);
+          if (m.place) {
+            m.place[i] = make_uint2(kNoCell, 0u);
+          }
           continue;
+        }
+        if (m.place) {
+          m.place[i] = make_uint2(Rc, Rl);
         }
         const float tau = __uint2float_rn(Rl) * m.tau_scale;
         const float a1  = A * tau, a2 = a1 * tau, a3 = a2 * tau;
@@ -296,6 +309,7 @@ namespace rg {
 
     struct SmoothAdjParams {
       SmoothMomParams m;
+      const uint2*    place; // a forward's placement record (single segment), or null: recompute
       const float4*   alpha; // nseg x nc
       float           inv_dln;
       float*          gw;
@@ -326,13 +340,25 @@ namespace rg {
         for (int c = 0; c < kComps; ++c) {
           v[c] = m.fp.comp[c] ? __ldg(m.fp.comp[c] + i) : 0.0f;
         }
-        float   gw = 0.0f, gu[3] = { 0.0f, 0.0f, 0.0f };
-        int64_t Q = 0;
-        float   A = 0.0f;
-        if (moment_particle_stage(v, m.fp, m.Pmin, m.Pmax, m.L, Q, A)) {
-          const uint64_t R   = static_cast<uint64_t>(m.Pmax - Q);
-          const uint32_t Rc  = static_cast<uint32_t>(R >> m.F);
-          const uint32_t Rl  = static_cast<uint32_t>(R) & mask;
+        float    gw = 0.0f, gu[3] = { 0.0f, 0.0f, 0.0f };
+        bool     live = false;
+        uint32_t Rc = 0, Rl = 0;
+        if (a.place) { // the forward placed this particle already
+          const uint2 pc = a.place[i];
+          live           = pc.x != kNoCell;
+          Rc             = pc.x;
+          Rl             = pc.y;
+        } else {
+          int64_t Q = 0;
+          float   A = 0.0f;
+          live      = moment_particle_stage(v, m.fp, m.Pmin, m.Pmax, m.L, Q, A);
+          if (live) {
+            const uint64_t R = static_cast<uint64_t>(m.Pmax - Q);
+            Rc               = static_cast<uint32_t>(R >> m.F);
+            Rl               = static_cast<uint32_t>(R) & mask;
+          }
+        }
+        if (live) {
           if (Rc < static_cast<uint32_t>(m.nc) && seg < m.nseg) {
             const float  tau = __uint2float_rn(Rl) * m.tau_scale;
             const float4 al  = __ldg(a.alpha + static_cast<int64_t>(seg) * m.nc + Rc);
@@ -480,12 +506,13 @@ namespace rg {
   }
 
   int smooth_moments_deposit(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off, int64_t n,
-                             int nseg, cudaStream_t s) {
+                             int nseg, cudaStream_t s, uint2* place) {
     if (n == 0 && !d_off) {
       return RG_OK;
     }
     SmoothMomParams m;
     fill_smooth_params(pl, comp, d_off, n, nseg, m);
+    m.place = d_off ? nullptr : place;
     int grid = 1;
     RG_TRY(particle_grid(n, grid));
     std::pair<cudaEvent_t, cudaEvent_t> ev { nullptr, nullptr };
@@ -532,7 +559,8 @@ namespace rg {
   // The adjoint through cell cubics: grad_out is nseg x nbins; gradients of the particles
   // [0, n) (one segment) or of the segments of d_off.
   int smooth_moments_adjoint(rg_spectrum_plan* pl, const float* const comp[kComps], const int64_t* d_off, int64_t n,
-                             int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s) {
+                             int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s,
+                             const uint2* place) {
     const int    nsg  = d_off ? nseg : 1;
     const size_t need = static_cast<size_t>(nsg) * pl->sm_cells;
     RG_TRY(smooth_reserve_cells(pl, need));
@@ -553,6 +581,7 @@ namespace rg {
     }
     SmoothAdjParams x {};
     fill_smooth_params(pl, comp, d_off, n, nseg, x.m);
+    x.place   = d_off ? nullptr : place;
     x.alpha   = reinterpret_cast<const float4*>(pl->d_cells);
     x.inv_dln = static_cast<float>(1.0 / pl->smooth->dln);
     x.gw      = gw;

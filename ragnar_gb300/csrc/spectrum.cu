@@ -1155,6 +1155,25 @@ int rg_spectrum_run(const rg_spectrum_plan* plan, const rg_particles* p, float* 
                        static_cast<cudaStream_t>(stream));
 }
 
+int rg_spectrum_run_placed(rg_spectrum_plan* plan, const rg_particles* p, float* out, void* placement,
+                           void* stream) {
+  rg::NvtxRange nvtx_range("SynchrotronSpectrum");
+  if (!plan || !placement || (!out && plan->nbins > 0) || plan->source != rg::kSrcParticles) {
+    return rg::set_error(RG_ERR_ARGUMENT, "rg_spectrum_run_placed: bad arguments");
+  }
+  RG_TRY(rg::check_particles(p));
+  if (plan->zero || plan->nbins == 0 || !plan->aligned || !rg::moments_selected(plan, 1)) {
+    return rg::set_error(RG_ERR_UNSUPPORTED,
+                         "rg_spectrum_run_placed: needs a plan that runs cell moments on its bin-aligned smooth table");
+  }
+  const float* comp[rg::kComps];
+  rg::particle_comps(p, comp);
+  auto s = static_cast<cudaStream_t>(stream);
+  RG_TRY(rg::moments_begin(plan, 1, s));
+  RG_TRY(rg::smooth_moments_deposit(plan, comp, nullptr, p->n, 1, s, static_cast<uint2*>(placement)));
+  return rg::moments_finish(plan, 1, out, s);
+}
+
 int rg_spectrum_run_batched(rg_spectrum_plan* plan, const rg_particles* p, const int64_t* offsets,
                             int32_t nseg, float* out, void* stream) {
   rg::NvtxRange nvtx_range("SynchrotronSpectrum");

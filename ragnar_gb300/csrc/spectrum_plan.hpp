@@ -95,10 +95,12 @@ namespace rg {
   int  smooth_align_plan(rg_spectrum_plan* pl, double ln_k0);
   int  smooth_moments_prepare(rg_spectrum_plan* pl, double ln_k0);
   int  smooth_reserve_cells(rg_spectrum_plan* pl, size_t entries);
+  // place: optional per-particle placement record (single-segment runs; see rg_spectrum_run_placed)
   int  smooth_moments_deposit(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
-                              int nseg, cudaStream_t s);
+                              int nseg, cudaStream_t s, uint2* place = nullptr);
   int  smooth_moments_finish(rg_spectrum_plan* pl, int nseg, float* out, cudaStream_t s);
   int  smooth_moments_adjoint(rg_spectrum_plan* pl, const float* const comp[10], const int64_t* d_off, int64_t n,
-                              int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s);
+                              int nseg, const float* grad_out, float* gw, float* const gu[3], cudaStream_t s,
+                              const uint2* place = nullptr);
 
 } // namespace rg

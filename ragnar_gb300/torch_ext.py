@@ -62,14 +62,21 @@ class _Spectrum(torch.autograd.Function):
         e = None if ex is None else [ex, ey, ez]
         prt = capi.particles([ux, uy, uz], b=[bx, by, bz], e=e, w=w, n=ux.numel())
         out = torch.empty(plan.nbins, device=dev, dtype=torch.float32)
-        plan.run(prt, out, _stream(dev))
+        # on cell-moment plans the forward records each particle's table placement (8 bytes per
+        # particle), which the backward then reads instead of placing the particle again
+        place = None
+        if plan.placement_supported():
+            place = torch.empty(2 * ux.numel(), device=dev, dtype=torch.int32)
+            plan.run_placed(prt, out, place, _stream(dev))
+        else:
+            plan.run(prt, out, _stream(dev))
         ctx.plan = plan
-        ctx.save_for_backward(w, ux, uy, uz, bx, by, bz, ex, ey, ez)
+        ctx.save_for_backward(w, ux, uy, uz, bx, by, bz, ex, ey, ez, place)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        w, ux, uy, uz, bx, by, bz, ex, ey, ez = ctx.saved_tensors
+        w, ux, uy, uz, bx, by, bz, ex, ey, ez, place = ctx.saved_tensors
         dev = ux.device
         need_w, need_u = ctx.needs_input_grad[1], any(ctx.needs_input_grad[2:5])
         gw = torch.empty_like(ux) if (need_w and w is not None) else None
@@ -78,7 +85,10 @@ class _Spectrum(torch.autograd.Function):
             return (None,) * 11
         e = None if ex is None else [ex, ey, ez]
         prt = capi.particles([ux, uy, uz], b=[bx, by, bz], e=e, w=w, n=ux.numel())
-        ctx.plan.adjoint(prt, grad_out.contiguous().float(), gw, gu, _stream(dev))
+        if place is not None:
+            ctx.plan.adjoint_placed(prt, place, grad_out.contiguous().float(), gw, gu, _stream(dev))
+        else:
+            ctx.plan.adjoint(prt, grad_out.contiguous().float(), gw, gu, _stream(dev))
         return (None, gw, gu[0], gu[1], gu[2], None, None, None, None, None, None)
 
 

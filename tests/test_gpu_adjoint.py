@@ -183,6 +183,49 @@ def test_autograd_end_to_end(gpu, oracle_lib, algo):
         assert np.max(np.abs(g - want)) / np.max(np.abs(want)) < 1e-3
 
 
+def test_placed_forward_and_adjoint_match_unplaced(gpu, oracle_lib):
+    """rg_spectrum_run_placed records each particle's table placement; the adjoint that reads
+    it equals the one that places the particles again bit for bit, and particles that add
+    nothing (zero field, huge energy) are recorded as such.  Plans that do not run cell
+    moments on an aligned smooth table refuse both calls."""
+    n, nbins = 20000, 200
+    P = particles(n, seed=53, bfield="iso", weights=True)
+    P["bx"][:50] = 0.0
+    P["by"][:50] = 0.0
+    P["bz"][:50] = 0.0  # W = 0: no emission
+    P["ux"][50:60] = 3e8  # e_peak far above the table
+    T = _device(P, gpu)
+    prt = capi.particles([T["ux"], T["uy"], T["uz"]], b=[T["bx"], T["by"], T["bz"]], w=T["w"])
+    plan = rt.spectrum_plan(oracle_lib.logspace(0.01, 1e7, nbins))
+    assert plan.placement_supported()
+    S0, S1 = torch.empty(nbins, device=gpu), torch.empty(nbins, device=gpu)
+    place = torch.full((2 * n,), -7, dtype=torch.int32, device=gpu)
+    plan.run(prt, S0)
+    plan.run_placed(prt, S1, place)
+    a64, b64 = S1.double(), S0.double()
+    assert bool(((a64 - b64).abs() <= 1.2e-7 * b64.abs().clamp(min=1e-300)).all())
+    rec = place.view(n, 2).cpu().numpy().view(np.uint32)
+    assert np.all(rec[:50, 0] == 0xFFFFFFFF) and np.all(rec[:50, 1] == 0)
+    assert not np.any(place.cpu().numpy() == -7)  # every particle written
+    gS = torch.rand(nbins, device=gpu)
+    g0 = [torch.empty(n, device=gpu) for _ in range(4)]
+    g1 = [torch.empty(n, device=gpu) for _ in range(4)]
+    plan.adjoint(prt, gS, g0[0], g0[1:])
+    plan.adjoint_placed(prt, place, gS, g1[0], g1[1:])
+    plan.check()
+    for a, b in zip(g0, g1):
+        assert torch.equal(a, b)
+    assert torch.all(g1[0][:50] == 0)
+    ref = capi.SpectrumPlan(oracle_lib.logspace(0.01, 1e7, nbins), 1.0, 1.0, 1.0)
+    assert not ref.placement_supported()
+    with pytest.raises(capi.RgError):
+        ref.run_placed(prt, S1, place)
+    with pytest.raises(capi.RgError):
+        ref.adjoint_placed(prt, place, gS, g1[0])
+    with pytest.raises(capi.RgError):
+        plan.run_placed(prt, S1, None)
+
+
 @pytest.mark.parametrize("algo", ALGOS)
 def test_batched_adjoint_matches_per_segment(gpu, oracle_lib, algo):
     P = particles(9000, seed=41, bfield="iso", weights=True)
