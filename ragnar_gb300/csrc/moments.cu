@@ -42,6 +42,7 @@
 #include <cmath>
 #include <limits>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 namespace rg {
@@ -70,6 +71,7 @@ namespace rg {
       int64_t         per_seg;
     };
 
+    template <bool kI32>
     __global__ void __launch_bounds__(kMomThreads) moments_deposit_kernel(const __grid_constant__ MomentParams m) {
       __shared__ int32_t  thr[kSliceBins];
       __shared__ uint16_t bucket[kMomBuckets + 1];
@@ -108,13 +110,16 @@ namespace rg {
       double2*       base   = m.hist + ms.z;
       const int64_t  first  = m.seg_off ? soff[0] : 0;
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
-      const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      // 32-bit particle indices when the stream allows it (the host checks last + stride < 2^32)
+      using Idx          = std::conditional_t<kI32, uint32_t, int64_t>;
+      const Idx  stride  = static_cast<Idx>(gridDim.x) * blockDim.x;
+      const Idx  i0      = static_cast<Idx>(first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+      const Idx  iend    = static_cast<Idx>(last);
       // this thread's segment, advanced as its particle index grows
-      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
-      for (int64_t i = i0; i < last; i += stride) {
+      int seg = m.seg_off ? segment_of(soff, m.nseg, static_cast<int64_t>(i0)) : 0;
+      for (Idx i = i0; i < iend; i += stride) {
         if (m.seg_off) {
-          while (seg < m.nseg && soff[seg + 1] <= i) {
+          while (seg < m.nseg && soff[seg + 1] <= static_cast<int64_t>(i)) {
             ++seg;
           }
         }
@@ -450,7 +455,11 @@ namespace rg {
       }
       RG_CUDA_TRY(cudaEventRecord(ev.first, s));
     }
-    moments_deposit_kernel<<<dim3(grid, pl->nslices), kMomThreads, 0, s>>>(m);
+    if (n + static_cast<int64_t>(grid) * kMomThreads < (int64_t(1) << 32)) {
+      moments_deposit_kernel<true><<<dim3(grid, pl->nslices), kMomThreads, 0, s>>>(m);
+    } else {
+      moments_deposit_kernel<false><<<dim3(grid, pl->nslices), kMomThreads, 0, s>>>(m);
+    }
     RG_CUDA_TRY(cudaGetLastError());
     if (pl->timing) {
       RG_CUDA_TRY(cudaEventRecord(ev.second, s));

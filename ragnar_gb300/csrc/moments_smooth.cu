@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 #include <vector>
 
 namespace rg {
@@ -89,6 +90,7 @@ namespace rg {
       return !__syncthreads_or(*m.fp.status != kDevOk);
     }
 
+    template <bool kI32>
     __global__ void __launch_bounds__(kSmThreads) smooth_deposit_kernel(const __grid_constant__ SmoothMomParams m) {
       __shared__ int64_t soff[kSmSharedSeg + 1];
       if (!stage_offsets(m, soff)) {
@@ -96,14 +98,17 @@ namespace rg {
       }
       const int64_t  first  = m.seg_off ? soff[0] : 0;
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
-      const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+      // 32-bit particle indices when the stream allows it (the host checks last + stride < 2^32)
+      using Idx            = std::conditional_t<kI32, uint32_t, int64_t>;
+      const Idx      stride = static_cast<Idx>(gridDim.x) * blockDim.x;
       const uint32_t mask   = (1u << m.F) - 1u;
-      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      const Idx      i0     = static_cast<Idx>(first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+      const Idx      iend   = static_cast<Idx>(last);
       // this thread's segment, advanced as its particle index grows
-      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
-      for (int64_t i = i0; i < last; i += stride) {
+      int seg = m.seg_off ? segment_of(soff, m.nseg, static_cast<int64_t>(i0)) : 0;
+      for (Idx i = i0; i < iend; i += stride) {
         if (m.seg_off) {
-          while (seg < m.nseg && soff[seg + 1] <= i) {
+          while (seg < m.nseg && soff[seg + 1] <= static_cast<int64_t>(i)) {
             ++seg;
           }
         }
@@ -316,6 +321,7 @@ namespace rg {
       float*          gu[3];
     };
 
+    template <bool kI32>
     __global__ void __launch_bounds__(kSmThreads) smooth_adjoint_kernel(const __grid_constant__ SmoothAdjParams a) {
       __shared__ int64_t     soff[kSmSharedSeg + 1];
       const SmoothMomParams& m = a.m;
@@ -324,14 +330,17 @@ namespace rg {
       }
       const int64_t  first  = m.seg_off ? soff[0] : 0;
       const int64_t  last   = m.seg_off ? soff[m.nseg] : m.n;
-      const int64_t  stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+      // 32-bit particle indices when the stream allows it (the host checks last + stride < 2^32)
+      using Idx            = std::conditional_t<kI32, uint32_t, int64_t>;
+      const Idx      stride = static_cast<Idx>(gridDim.x) * blockDim.x;
       const uint32_t mask   = (1u << m.F) - 1u;
-      const int64_t  i0     = first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      const Idx      i0     = static_cast<Idx>(first + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+      const Idx      iend   = static_cast<Idx>(last);
       // this thread's segment, advanced as its particle index grows
-      int seg = m.seg_off ? segment_of(soff, m.nseg, i0) : 0;
-      for (int64_t i = i0; i < last; i += stride) {
+      int seg = m.seg_off ? segment_of(soff, m.nseg, static_cast<int64_t>(i0)) : 0;
+      for (Idx i = i0; i < iend; i += stride) {
         if (m.seg_off) {
-          while (seg < m.nseg && soff[seg + 1] <= i) {
+          while (seg < m.nseg && soff[seg + 1] <= static_cast<int64_t>(i)) {
             ++seg;
           }
         }
@@ -527,7 +536,11 @@ namespace rg {
       }
       RG_CUDA_TRY(cudaEventRecord(ev.first, s));
     }
-    smooth_deposit_kernel<<<grid, kSmThreads, 0, s>>>(m);
+    if (n + static_cast<int64_t>(grid) * kSmThreads < (int64_t(1) << 32)) {
+      smooth_deposit_kernel<true><<<grid, kSmThreads, 0, s>>>(m);
+    } else {
+      smooth_deposit_kernel<false><<<grid, kSmThreads, 0, s>>>(m);
+    }
     RG_CUDA_TRY(cudaGetLastError());
     if (pl->timing) {
       RG_CUDA_TRY(cudaEventRecord(ev.second, s));
@@ -591,7 +604,11 @@ namespace rg {
     }
     int grid = 1;
     RG_TRY(particle_grid(n, grid));
-    smooth_adjoint_kernel<<<grid, kSmThreads, 0, s>>>(x);
+    if (n + static_cast<int64_t>(grid) * kSmThreads < (int64_t(1) << 32)) {
+      smooth_adjoint_kernel<true><<<grid, kSmThreads, 0, s>>>(x);
+    } else {
+      smooth_adjoint_kernel<false><<<grid, kSmThreads, 0, s>>>(x);
+    }
     RG_CUDA_TRY(cudaGetLastError());
     return RG_OK;
   }
