@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the side cases (plain kernel, batched graph, adjoint, GEMM, Adam fit, histogram, "
                          "IC, the drop-in module calls)")
+    ap.add_argument("--ref-seconds", type=float, default=90.0,
+                    help="CPU seconds the reference arm spreads over its warm-up and timed steps")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--profile-case", nargs="?", const="spectrum",
@@ -281,7 +283,7 @@ def run_reference_arm(args, rank):
     t0 = time.perf_counter()
     fn(calib, bins)
     rate = 20000 * NBINS / max(time.perf_counter() - t0, 1e-6)
-    per_step = max(90.0 / max(args.steps + args.warmup, 1), 0.2)
+    per_step = max(args.ref_seconds / max(args.steps + args.warmup, 1), 0.2)
     n = int(min(max(rate * per_step / NBINS, 20000), 2e7))
     P = make_particles_numpy(n, seed=9)
     for _ in range(args.warmup):
