@@ -17,8 +17,8 @@
 // bin, and bin b reads segment Rc - Dc_b (Dc_b = (Pmax >> F) - t_b).  The forward is
 //   S_b / e_b = sum_cells sum_j c'_j(Rc - Dc_b) M_j(Rc),  M_j = sum_p A_p tau_p^j,
 //   c'_j = c_j + eps_b (j + 1) c_{j+1}   (first order in eps_b: F(tau + eps)),
-// four FP64 moments per cell (deposited into 32 slots per cell, which spreads the
-// atomics of crowded cells, then folded), and the adjoint of a loss L with
+// four FP64 moments per cell (deposited into 64 slots per cell, which spreads the
+// atomics of crowded cells, then folded into a compact cell table), and the adjoint of a loss L with
 // G_b = dL/dS_b is, per particle, the cubic of its cell
 //   R1(tau) = sum_b G_b e_b F_b(tau) = sum_j alpha_j(Rc) tau^j,
 //   alpha_j(c) = sum_b G_b e_b c'_j(c - Dc_b),   R2 = (dR1/dtau) / dln,
