@@ -1307,7 +1307,8 @@ def profile_case_200():
 def profile_case_smooth(algo=1, n=1 << 22):
     """The differentiable path on n particles (|u| ~ u^-2 on [1, 100], isotropic, B = z,
     w = 1) x 512 bins 0.01..1e7 with the smooth table: 4 forward and 4 adjoint runs, by
-    the fused kernels (algo 1) or the cell moments (algo 2)."""
+    the fused kernels (algo 1) or the cell moments (algo 2, with the placement record the
+    forward writes for the adjoint)."""
     import torch  # noqa: PLC0415
 
     from ragnar_gb300 import capi  # noqa: PLC0415
@@ -1325,9 +1326,14 @@ def profile_case_smooth(algo=1, n=1 << 22):
     gw = torch.empty(n, device=device)
     gu = [torch.empty(n, device=device) for _ in range(3)]
     stream = torch.cuda.current_stream().cuda_stream
+    place = torch.empty(2 * n, device=device, dtype=torch.int32) if plan.placement_supported() else None
     for _ in range(4):
-        plan.run(prt, out, stream)
-        plan.adjoint(prt, gS, gw, gu, stream)
+        if place is not None:  # the torch_ext path: the forward records the placements the adjoint reads
+            plan.run_placed(prt, out, place, stream)
+            plan.adjoint_placed(prt, place, gS, gw, gu, stream)
+        else:
+            plan.run(prt, out, stream)
+            plan.adjoint(prt, gS, gw, gu, stream)
     torch.cuda.synchronize()
     plan.check()
     plan.close()
