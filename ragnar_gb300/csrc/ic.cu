@@ -57,6 +57,8 @@ namespace rg {
       const float* inv4es;  // ns: 1 / (4 e_s)
       const float* inv4es_min; // min over s of 1 / (4 e_s) (positive values), one float
       const float* ws;      // ns: f_s / e_s
+      const float4* setup;  // ng x ne_pad per (gamma bin, IC bin): (pg, 1 + h, B1, 0), or null
+      int          ne_pad;  // nslices x slice_w
       int          ns;
       const float* eic;     // ne IC photon energies
       int          ne;
@@ -82,6 +84,50 @@ namespace rg {
       }
     }
 
+    // L = 2 ln 2 rounded to FP32; log2 L and -2 / L^2 of that FP32 value
+    constexpr float kIcL     = 1.3862943649291992f;
+    constexpr float kIcLog2L = 0.47123363101939075f;
+
+    // What an (IC bin, gamma bin) pair contributes to every eval: pg = L t / g (p = pg / (4 e_s)),
+    // 1 + h, and the linear coefficient (1 - h) / L - log2 L; pg = inf for a pair that no soft
+    // photon reaches (e >= g or an invalid e).  e: the bin's energy, 0 if invalid.
+    __device__ __forceinline__ float4 ic_pair_setup(float e, float gv, float inv_g, float tg_floor) {
+      const float d     = __fsub_rn(gv, e);
+      const bool  reach = e > 0.0f && d > 0.0f;
+      float       t = 0.0f, h = 0.0f;
+      if (reach) {
+        t = __fdiv_rn(e, d);
+        h = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(t, t)), __fadd_rn(1.0f, t));
+      }
+      const float pg = reach ? __fmul_rn(kIcL, fmaxf(__fmul_rn(t, inv_g), tg_floor)) : __int_as_float(0x7f800000);
+      return make_float4(pg, __fadd_rn(1.0f, h), __fsub_rn(__fdiv_rn(__fsub_rn(1.0f, h), kIcL), kIcLog2L), 0.0f);
+    }
+
+    __device__ __forceinline__ float ic_bin_energy(const IcParams& p, int bin) {
+      const float e = bin < p.ne ? __ldg(p.eic + bin) : 0.0f;
+      return (e > 0.0f && isfinite(e)) ? e : 0.0f;
+    }
+
+    // t/g >= this keeps q = (t/g) / (4 e_s) >= 1e-30 for every soft photon with e_s > 0: the
+    // log's argument stays a normal float without a per-eval clamp
+    __device__ __forceinline__ float ic_tg_floor(const IcParams& p) {
+      return __fdiv_rn(1e-30f, *p.inv4es_min);
+    }
+
+    // The pair setups of every (gamma bin, padded IC bin), once per call: the main kernel's
+    // items (gamma bin, 64 soft photons) would otherwise repeat them for every chunk.
+    __global__ void ic_setup_kernel(const __grid_constant__ IcParams p, float4* __restrict__ setup) {
+      const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (t >= static_cast<int64_t>(p.ng) * p.ne_pad) {
+        return;
+      }
+      const int   g   = static_cast<int>(t / p.ne_pad), bin = static_cast<int>(t % p.ne_pad);
+      const float gv  = __ldg(p.gb + g);
+      // invalid gamma bins are skipped by the main kernel before it reads their row
+      setup[t] = (gv > 0.0f && isfinite(gv)) ? ic_pair_setup(ic_bin_energy(p, bin), gv, __frcp_rn(gv), ic_tg_floor(p))
+                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+
     template <int K>
     __global__ void __launch_bounds__(kIcThreads, 2) ic_kernel(const __grid_constant__ IcParams p) {
       const int     lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -93,24 +139,15 @@ namespace rg {
 
       // this lane's IC energy of row k (0 for padding and for invalid bins); reloaded
       // where needed (per item) instead of held in registers
-      auto energy = [&](int k) -> float {
-        const int   bin = slice * (K * 32) + k * 32 + lane;
-        const float e   = bin < p.ne ? __ldg(p.eic + bin) : 0.0f;
-        return (e > 0.0f && isfinite(e)) ? e : 0.0f;
-      };
+      auto energy = [&](int k) -> float { return ic_bin_energy(p, slice * (K * 32) + k * 32 + lane); };
       float hi[K], lo[K];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         hi[k] = 0.0f;
         lo[k] = 0.0f;
       }
-      // L = 2 ln 2 rounded to FP32; log2 L and -2 / L^2 of that FP32 value
-      const float kL     = 1.3862943649291992f;
-      const float kLog2L = 0.47123363101939075f;
-      const float kC2    = -1.0406844847835448f;
-      // t/g >= this keeps q = (t/g) / (4 e_s) >= 1e-30 for every soft photon with e_s > 0:
-      // the log's argument stays a normal float without a per-eval clamp
-      const float tg_floor = __fdiv_rn(1e-30f, *p.inv4es_min);
+      const float kC2      = -1.0406844847835448f; // -2 / L^2
+      const float tg_floor = ic_tg_floor(p);
 
       for (int64_t it = i0 + warp; it < i1; it += kIcWarps) {
         const int   g     = static_cast<int>(it / nsc);
@@ -122,23 +159,16 @@ namespace rg {
           continue; // non-positive or non-finite gamma bins contribute nothing (warp-uniform)
         }
         const float inv_g = __frcp_rn(gv);
-        // per (e, g): pg = L t / g, 1 + h, 1 - h; q = (t / g) / (4 e_s) > 1 marks no
-        // contribution, and so does pg = inf for a pair that no soft photon reaches
+        // per (e, g): pg, 1 + h and the linear coefficient (ic_pair_setup), from the call's
+        // setup table when there is one; q = (t / g) / (4 e_s) > 1 marks no contribution
         float pg[K], A0[K], B1[K], acc[K];
+        const float4* su = p.setup ? p.setup + static_cast<int64_t>(g) * p.ne_pad + slice * (K * 32) + lane : nullptr;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-          const float e = energy(k);
-          const float d = __fsub_rn(gv, e);
-          const bool  reach = e > 0.0f && d > 0.0f;
-          float       t = 0.0f, h = 0.0f;
-          if (reach) {
-            t = __fdiv_rn(e, d);
-            h = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(t, t)), __fadd_rn(1.0f, t));
-          }
-          pg[k]  = reach ? __fmul_rn(kL, fmaxf(__fmul_rn(t, inv_g), tg_floor)) // p = pg / (4 e_s)
-                         : __int_as_float(0x7f800000);
-          A0[k]  = __fadd_rn(1.0f, h);
-          B1[k]  = __fsub_rn(__fdiv_rn(__fsub_rn(1.0f, h), kL), kLog2L);
+          const float4 v = su ? __ldg(su + k * 32) : ic_pair_setup(energy(k), gv, inv_g, tg_floor);
+          pg[k]  = v.x;
+          A0[k]  = v.y;
+          B1[k]  = v.z;
           acc[k] = 0.0f;
         }
         for (int s = s0; s < s1; ++s) {
@@ -263,7 +293,12 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   const size_t off_ws   = 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_min  = off_ws + 256 * ((sizeof(float) * ns + 255) / 256);
   const size_t off_part = off_min + 256;
-  const size_t bytes    = off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * slice_w;
+  // the (gamma bin, IC bin) setup table when it is small (it is 16 bytes per pair)
+  const int64_t ne_pad    = static_cast<int64_t>(nslices) * slice_w;
+  const size_t  set_bytes = sizeof(float4) * static_cast<size_t>(ng) * static_cast<size_t>(ne_pad);
+  const bool    use_setup = set_bytes <= (size_t(64) << 20);
+  const size_t  off_set   = 256 * ((off_part + sizeof(double) * static_cast<size_t>(grid) * nslices * slice_w + 255) / 256);
+  const size_t  bytes     = off_set + (use_setup ? set_bytes : 0);
   unsigned char* buf    = nullptr;
   RG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, s));
   rg::IcParams p {};
@@ -279,6 +314,8 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
   p.nslices    = nslices;
   p.slice_w    = slice_w;
   p.partials   = reinterpret_cast<double*>(buf + off_part);
+  p.ne_pad     = static_cast<int>(ne_pad);
+  p.setup      = nullptr;
   p.inv4es_min = reinterpret_cast<float*>(buf + off_min);
   // the minimum slot starts at 0x7f7f7f7f (3.4e38, above any 1 / (4 e_s) of a positive float)
   cudaError_t e = cudaMemsetAsync(buf + off_min, 0x7f, sizeof(unsigned), s);
@@ -287,6 +324,13 @@ int rg_ic_spectrum(const float* gbins, const float* f, int32_t ng, int32_t log_s
                                                          reinterpret_cast<float*>(buf + off_ws),
                                                          reinterpret_cast<unsigned*>(buf + off_min));
     e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && use_setup) {
+    auto* setup  = reinterpret_cast<float4*>(buf + off_set);
+    const int64_t pairs = static_cast<int64_t>(ng) * ne_pad;
+    rg::ic_setup_kernel<<<static_cast<unsigned>((pairs + 255) / 256), 256, 0, s>>>(p, setup);
+    e       = cudaGetLastError();
+    p.setup = setup;
   }
   if (e == cudaSuccess) e = rg::launch_ic(K, p, dim3(grid, nslices), s);
   if (e == cudaSuccess) {
