@@ -88,6 +88,18 @@ def test_wide_and_masked_soft_photons(gpu, oracle_lib):
     assert max_rel(got, want) <= SPECTRUM_RTOL
 
 
+def test_large_grid_without_setup_table(gpu, oracle_lib):
+    """8192 gamma bins x 1024 IC bins: the per-call (gamma bin, IC bin) setup table would take
+    134 MB, above its 64 MB cap, so the kernel computes each pair's setup per item instead."""
+    gb = oracle_lib.logspace(10.0, 1e6, 8192)
+    fp = (gb.astype(np.float64) ** -2.0 * np.exp(-gb / 3e5)).astype(np.float32)
+    es = oracle_lib.logspace(1e-9, 1e-5, 16)
+    fs = np.ones(16, np.float32)
+    eic = oracle_lib.logspace(1e-3, 1e6, 1024)
+    got = gpu_ic(gb, fp, True, es, fs, eic, gpu)
+    assert max_rel(got, oracle_lib.ic_spectrum_f64(gb, fp, True, es, fs, eic)) <= SPECTRUM_RTOL
+
+
 def test_empty_inputs(gpu):
     dev = gpu
     z = torch.zeros(4, device=dev)
