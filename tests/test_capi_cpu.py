@@ -162,3 +162,15 @@ def test_particle_structs_keep_their_arrays():
     del a
     gc.collect()
     assert ref() is not None and h.u[0] == ref().ctypes.data
+
+
+def test_placed_entry_points_reject_bad_arguments():
+    """The placed forward and adjoint check their arguments before any device work: no plan,
+    no placement buffer or no gradient input is RG_ERR_ARGUMENT with a message."""
+    L = capi.lib()
+    p = capi.particles([16, 32, 48], n=4)  # addresses only; nothing is read
+    assert L.rg_spectrum_run_placed(None, ctypes.byref(p), 8, 8, None) == capi.RG_ERR_ARGUMENT
+    assert b"rg_spectrum_run_placed" in L.rg_last_error()
+    assert L.rg_spectrum_adjoint_placed(None, ctypes.byref(p), 8, 8, None, None, None, None,
+                                        None) == capi.RG_ERR_ARGUMENT
+    assert b"rg_spectrum_adjoint_placed" in L.rg_last_error()
